@@ -1,0 +1,375 @@
+"""Benchmark: 30-qubit, 40-layer random circuit (2260 gates incl. QFT) on one GB300.
+
+Workload (the configuration the headline metric is quoted on): 2^30 complex
+amplitudes, |+>^30 initial state, 40 layers of one random single-qubit gate
+per qubit (H,X,Y,Z,S,T,RX,RY,RZ,P; seed 0) plus a CNOT brickwork, then the
+QFT on all 30 qubits.  Synthetic, seeded data (no dataset is involved).
+
+One step = one execution of the whole circuit on the resident state
+(state reset to |+>^30, then the fused complex-FP32 plan).  The metric is
+layers/s (40 layers per step).  Inputs (8 GiB of FP32 amplitudes) are far
+larger than the 129 MB L2, so no L2 flush is needed between steps.
+
+Besides the JSON keys the contract requires, the line carries the plain FP64
+per-gate CUDA path (the >= 8x target's denominator), the complex-FP32
+per-gate path, and the fused path's infidelity against the FP64 per-gate
+result (FP64 accumulation on the device).
+
+--impl reference times the reference implementation's CPU data flow (the
+oracle port of the rayon branch, oracle/qi_oracle.cpp) on a bounded sample.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_QUBITS = 30
+LAYERS = 40
+SEED = 0
+FUSED_K = 6
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
+    ap.add_argument("--qubits", type=int, default=N_QUBITS)
+    ap.add_argument("--skip-baselines", action="store_true", help="skip FP64/FP32 per-gate and CPU legs")
+    return ap.parse_args()
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index):
+        self.dev = device_index
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", "clocks_bench.csv")
+
+    def start(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.dev), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_port_sample(n, gates, budget_gates, threads):
+    """Time the oracle port of the reference's rayon data flow on the first
+    `budget_gates` gates at n qubits; returns (seconds per gate, gates timed, n)."""
+    import numpy as np
+    from oracle import oracle as orc
+    from quant_iron_gb300 import workloads
+    init = workloads.plus_state(n)
+    _, secs = orc.port_execute(init, n, gates[:budget_gates], threads)
+    del init
+    return secs / budget_gates
+
+
+def host_mem_gb():
+    try:
+        for line in open("/proc/meminfo"):
+            if line.startswith("MemAvailable:"):
+                return int(line.split()[1]) / 1e6
+    except Exception:
+        pass
+    return 0.0
+
+
+def cpu_baseline(n, gates, budget_s=25.0):
+    """Bounded sample of the reference CPU data flow; picks the gate count to stay near budget_s."""
+    threads = os.cpu_count() or 1
+    # the rayon data flow holds ~56 B/amp (state, clone, update list); fall back to fewer qubits if short
+    need_gb = (1 << n) * 60 / 1e9
+    nn = n
+    while nn > 20 and host_mem_gb() < need_gb * 1.3:
+        nn -= 1
+        need_gb = (1 << nn) * 60 / 1e9
+    from quant_iron_gb300 import workloads
+    g = gates if nn == n else workloads.random_circuit(nn, LAYERS, seed=SEED)
+    t1 = cpu_port_sample(nn, g, 1, threads)
+    k = max(1, min(len(g) - 1, int(budget_s / max(t1, 1e-6)) - 1))
+    tk = cpu_port_sample(nn, g[1:], k, threads) if k > 0 else t1
+    per_gate = tk * (1 << (n - nn))   # scale a smaller sample to n qubits by amplitude count
+    step_s = per_gate * len(gates)
+    return {"value": LAYERS / step_s, "unit": "layers/s", "cores": threads, "kind": "port",
+            "sample": "oracle port of the reference rayon data flow (clone + per-pair update list + serial "
+                      "scatter): %d gates of the %d-qubit circuit timed, extrapolated to all %d gates%s" %
+                      (k + 1, nn, len(gates), "" if nn == n else " and scaled by 2^%d amplitudes" % (n - nn)),
+            "seconds_per_gate": per_gate}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    sys.path.insert(0, ROOT)
+    import __graft_entry__ as ge
+    ge.build_oracle()
+    ge.load_package()
+    from quant_iron_gb300 import workloads
+    n = args.qubits
+    gates = workloads.random_circuit(n, LAYERS, seed=SEED)
+    threads = os.cpu_count() or 1
+    need_gb = (1 << n) * 60 / 1e9
+    nn = n
+    while nn > 20 and host_mem_gb() < need_gb * 1.3:
+        nn -= 1
+        need_gb = (1 << nn) * 60 / 1e9
+    g = gates if nn == n else workloads.random_circuit(nn, LAYERS, seed=SEED)
+    per_step_gates = 2
+    for _ in range(args.warmup):
+        cpu_port_sample(nn, g, 1, threads)
+    times = []
+    for s in range(args.steps):
+        off = (s * per_step_gates) % (len(g) - per_step_gates)
+        times.append(cpu_port_sample(nn, g[off:], per_step_gates, threads))
+    per_gate = statistics.mean(times) * (1 << (n - nn))
+    step_s = per_gate * len(gates)
+    value = LAYERS / step_s
+    sample = ("oracle port of the reference rayon data flow on %d host threads: %d gates of the %d-qubit circuit per "
+              "step, extrapolated to all %d gates%s" % (threads, per_step_gates, nn, len(gates),
+                                                       "" if nn == n else " and scaled by 2^%d" % (n - nn)))
+    line = {"impl": "reference", "metric": "layers/s", "value": value, "unit": "layers/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_s * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic",
+            "config": {"workload": "random circuit, %d qubits, %d layers + QFT (%d gates), seed %d" %
+                                   (n, LAYERS, len(gates), SEED), "qubits": n, "layers": LAYERS},
+            "cpu_baseline": {"value": value, "unit": "layers/s", "cores": threads, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": "layers/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    import numpy as np
+    import torch
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    import __graft_entry__ as ge
+    ge.build()
+    qi = ge.load_package()
+    from quant_iron_gb300 import workloads
+    qi._abi.check(qi._abi.lib.qi_set_device(local))
+
+    n = args.qubits
+    gates = workloads.random_circuit(n, LAYERS, seed=SEED)
+    terms = workloads.heisenberg_open_chain(n, seed=SEED)
+    t0 = time.perf_counter()
+    plan = qi.Plan(n, qi.F32, gates, fusion=qi.FUSION_GREEDY, max_block_qubits=FUSED_K)
+    plan_s = time.perf_counter() - t0
+    stats = plan.stats()
+    stream = torch.cuda.Stream()
+    st = qi.DeviceState(n, qi.F32)
+    st.set_stream(stream.cuda_stream)
+
+    def step():
+        st.set_plus()
+        plan.execute(st)
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+
+    for _ in range(args.warmup):
+        step()
+    barrier()
+    clocks = ClockSampler(local)
+    clocks.start()
+    l0 = qi.launch_count()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier()
+    with torch.cuda.stream(stream):
+        ev0.record(stream)
+        for _ in range(args.steps):
+            step()
+        ev1.record(stream)
+    barrier()
+    launches = qi.launch_count() - l0
+    clk = clocks.stop()
+    ms = ev0.elapsed_time(ev1)
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_per_step = ms / args.steps
+    value = world * LAYERS * args.steps / (ms / 1e3)
+
+    # per-op device times of one execution (events on the launching stream)
+    ops, op_ms = qi.plan_profile(plan, st)
+    by_kernel = {}
+    for op, t in zip(ops, op_ms):
+        name = qi.KERNEL_OF_OP_KIND.get(op["kind"], str(op["kind"]))
+        d = by_kernel.setdefault(name, {"launches": 0, "ms": 0.0})
+        d["launches"] += 1
+        d["ms"] += t
+    dom = max(by_kernel, key=lambda k: by_kernel[k]["ms"])
+    peak, peak_kind = load_peaks()
+    pass_bytes = (1 << n) * 8 * 2   # one read + one write of every FP32 amplitude
+    avg_ms = by_kernel[dom]["ms"] / by_kernel[dom]["launches"]
+    achieved = pass_bytes / (avg_ms / 1e3) / 1e9
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": None, "kernel": dom, "peak_source": peak_kind,
+                "algorithmic_bytes_per_launch": pass_bytes, "avg_launch_ms": avg_ms,
+                "kernels": {k: {"launches": v["launches"], "ms": round(v["ms"], 3),
+                                "share": round(v["ms"] / max(1e-9, sum(x["ms"] for x in by_kernel.values())), 4)}
+                            for k, v in by_kernel.items()}}
+
+    # energy of the final state (FP64 reduction)
+    energy = qi.sumop_expectation(st, terms).real
+
+    extra = {}
+    if rank == 0 and not args.skip_baselines:
+        # plain FP64 per-gate CUDA path (the denominator of the >= 8x target) and FP32 per-gate
+        plan64 = qi.Plan(n, qi.F64, gates, fusion=qi.FUSION_NONE)
+        s64 = qi.DeviceState(n, qi.F64)
+        s64.set_stream(stream.cuda_stream)
+        s64.set_plus()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        plan64.execute(s64)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms64 = e0.elapsed_time(e1)
+        energy64 = qi.sumop_expectation(s64, terms).real
+        # infidelity of the fused FP32 result against the FP64 per-gate result
+        st.set_plus()
+        plan.execute(st)
+        tmp = qi.DeviceState(n, qi.F32)
+        tmp.set_stream(stream.cuda_stream)
+        tmp.copy_from(s64)
+        ov = tmp.inner_product(st)
+        infid = 1.0 - abs(ov) ** 2 / (tmp.norm_sqr() * st.norm_sqr())
+        # max amplitude error on a sampled stride of amplitudes
+        idx = np.linspace(0, (1 << n) - 1, 4096).astype(np.int64)
+        max_err = max(abs(st.amplitude(int(i)) - s64.amplitude(int(i))) for i in idx[:256])
+        tmp.close()
+        s64.close()
+        del plan64
+        plan32 = qi.Plan(n, qi.F32, gates, fusion=qi.FUSION_NONE)
+        st.set_plus()
+        torch.cuda.synchronize()
+        e0.record(stream)
+        plan32.execute(st)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms32 = e0.elapsed_time(e1)
+        del plan32
+        extra = {"fp64_per_gate_ms": ms64, "fp32_per_gate_ms": ms32, "fused_fp32_ms": ms_per_step,
+                 "speedup_fused_vs_fp64_per_gate": ms64 / ms_per_step,
+                 "infidelity_fused_vs_fp64": infid, "max_amp_error_sampled": max_err,
+                 "energy_fused_fp32": energy, "energy_fp64_per_gate": energy64,
+                 "energy_error": abs(energy - energy64),
+                 "gates_per_s_fused": len(gates) / (ms_per_step / 1e3)}
+
+    # end-to-end through the public API with host buffers: H2D of the initial state,
+    # the circuit, D2H of the final state, every step
+    e2e = None
+    if rank == 0:
+        dim = 1 << n
+        host_in = torch.empty(2 * dim, dtype=torch.float64, pin_memory=True)
+        host_in.fill_(1.0 / (dim ** 0.5))
+        host_in[1::2] = 0.0
+        two_buffers = host_mem_gb() > 3 * 16 * dim / 1e9
+        host_out = torch.empty(2 * dim, dtype=torch.float64, pin_memory=True) if two_buffers else host_in
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        e2e_steps = max(1, min(args.steps, 3))
+        for _ in range(e2e_steps):
+            st.upload_ptr(host_in.data_ptr(), dim)
+            plan.execute(st)
+            st.download_ptr(host_out.data_ptr(), dim)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+        e2e_ms = e0.elapsed_time(e1)
+        e2e = {"value": LAYERS * e2e_steps / (e2e_ms / 1e3), "unit": "layers/s", "h2d_bytes_per_step": 16 * dim,
+               "d2h_bytes_per_step": 16 * dim, "wall_s": wall, "steps": e2e_steps}
+        del host_in, host_out
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.skip_baselines:
+        st.close()
+        cpu = cpu_baseline(n, gates)
+
+    if rank == 0:
+        line = {"metric": "layers/s", "value": value, "unit": "layers/s", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "c64", "data": "synthetic",
+                "config": {"workload": "random circuit, %d qubits, %d layers + QFT (%d gates), |+>^%d, seed %d; "
+                                       "fused complex-FP32 blocks k<=%d" % (n, LAYERS, len(gates), n, SEED, FUSED_K),
+                           "qubits": n, "layers": LAYERS, "gates": len(gates), "fusion": "greedy k<=%d" % FUSED_K,
+                           "plan": stats, "plan_build_s": plan_s,
+                           "l2": "inputs (%d GiB state) larger than the 129 MB L2; no flush" % ((1 << n) * 8 >> 30),
+                           "parallelism": "replicas" if world > 1 else "single GPU"},
+                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk, "gpu_launches": launches}
+        line.update(extra)
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

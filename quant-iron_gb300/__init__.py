@@ -1,0 +1,305 @@
+"""quant-iron GB300 state-vector engine — Python binding of the C ABI.
+
+The engine itself is `lib/libqi_gb300.so` (CUDA, sm_103a).  This package is a
+thin ctypes layer over include/qi_engine.h:
+
+  DeviceState        a device-resident state handle (qi_state_*)
+  Plan               a compiled circuit (qi_plan_*), fused or per-gate
+  circuit_execute    Circuit::execute on a resident state
+  sumop_expectation / sumop_apply / pauli_* / trotter_evolve
+
+`quant_iron` (the submodule) mirrors the reference crate's public API —
+State, the Operator types, PauliString, SumOp, Circuit — on top of it.
+"""
+import ctypes
+
+import numpy as np
+
+from . import _abi
+from ._abi import (F32, F64, FUSION_GREEDY, FUSION_LEARNED, FUSION_NONE, GATE_DTYPE, TERM_DTYPE, QuantIronError,
+                   check, lib)
+
+__all__ = ["DeviceState", "Plan", "circuit_execute", "sumop_expectation", "sumop_apply", "trotter_evolve",
+           "launch_count", "F32", "F64", "FUSION_NONE", "FUSION_GREEDY", "FUSION_LEARNED", "QuantIronError"]
+
+
+def launch_count():
+    """Kernels launched by the engine since it was loaded."""
+    return int(lib.qi_launch_count())
+
+
+def version():
+    return lib.qi_version().decode()
+
+
+def _as_c128(v):
+    v = np.ascontiguousarray(v, dtype=np.complex128)
+    return v
+
+
+class DeviceState:
+    """A 2^n-amplitude state resident in GPU memory (complex FP64 or FP32)."""
+
+    def __init__(self, num_qubits, precision=F64):
+        self.h = ctypes.c_void_p()
+        check(lib.qi_state_create(int(num_qubits), int(precision), ctypes.byref(self.h)))
+        self.n = int(num_qubits)
+        self.precision = int(precision)
+
+    @property
+    def dim(self):
+        return 1 << self.n
+
+    def close(self):
+        if self.h:
+            lib.qi_state_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def set_stream(self, stream_handle):
+        check(lib.qi_state_set_stream(self.h, ctypes.c_void_p(int(stream_handle) if stream_handle else 0)))
+
+    def stream(self):
+        s = ctypes.c_void_p()
+        check(lib.qi_state_get_stream(self.h, ctypes.byref(s)))
+        return s.value or 0
+
+    def device_ptr(self):
+        p = ctypes.c_void_p()
+        check(lib.qi_state_device_ptr(self.h, ctypes.byref(p)))
+        return p.value
+
+    def synchronize(self):
+        check(lib.qi_state_synchronize(self.h))
+
+    def upload(self, amps):
+        a = _as_c128(amps)
+        if a.size != self.dim:
+            raise ValueError("expected %d amplitudes, got %d" % (self.dim, a.size))
+        check(lib.qi_state_upload(self.h, a.ctypes.data, a.size))
+
+    def upload_ptr(self, host_ptr, num_amps):
+        """Upload from a raw host pointer (e.g. pinned memory) of interleaved f64 pairs."""
+        check(lib.qi_state_upload(self.h, ctypes.c_void_p(host_ptr), int(num_amps)))
+
+    def download(self, out=None):
+        if out is None:
+            out = np.empty(self.dim, dtype=np.complex128)
+        check(lib.qi_state_download(self.h, out.ctypes.data, out.size))
+        return out
+
+    def download_ptr(self, host_ptr, num_amps):
+        check(lib.qi_state_download(self.h, ctypes.c_void_p(host_ptr), int(num_amps)))
+
+    def set_zero(self):
+        check(lib.qi_state_set_zero(self.h))
+
+    def set_basis(self, n):
+        check(lib.qi_state_set_basis(self.h, int(n)))
+
+    def set_plus(self):
+        check(lib.qi_state_set_plus(self.h))
+
+    def set_minus(self):
+        check(lib.qi_state_set_minus(self.h))
+
+    def set_ghz(self):
+        check(lib.qi_state_set_ghz(self.h))
+
+    def check_normalised(self):
+        check(lib.qi_state_check_normalised(self.h))
+
+    def copy_from(self, other):
+        check(lib.qi_state_copy(self.h, other.h))
+
+    def scale(self, c):
+        c = complex(c)
+        check(lib.qi_state_scale(self.h, c.real, c.imag))
+
+    def axpy(self, a, x):
+        a = complex(a)
+        check(lib.qi_state_axpy(self.h, a.real, a.imag, x.h))
+
+    def inner_product(self, other):
+        out = (ctypes.c_double * 2)()
+        check(lib.qi_state_inner_product(self.h, other.h, out))
+        return complex(out[0], out[1])
+
+    def norm_sqr(self):
+        out = ctypes.c_double()
+        check(lib.qi_state_norm_sqr(self.h, ctypes.byref(out)))
+        return out.value
+
+    def normalise(self):
+        check(lib.qi_state_normalise(self.h))
+
+    def amplitude(self, idx):
+        out = (ctypes.c_double * 2)()
+        check(lib.qi_state_amplitude(self.h, int(idx), out))
+        return complex(out[0], out[1])
+
+    def apply_gate(self, gate_row):
+        g = np.ascontiguousarray(gate_row, dtype=GATE_DTYPE).reshape(())
+        check(lib.qi_apply_gate(self.h, g.ctypes.data))
+
+
+def tensor_product(out, a, b):
+    check(lib.qi_state_tensor_product(out.h, a.h, b.h))
+
+
+def _options(fusion, max_block_qubits=0, use_tensor_cores=0):
+    return _abi.ExecOptions(int(fusion), int(max_block_qubits), int(use_tensor_cores), 0)
+
+
+def _theta_arg(theta):
+    if theta is None:
+        return None, 0, None
+    t = np.ascontiguousarray(theta, dtype=np.float64)
+    return t.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), t.size, t
+
+
+class Plan:
+    """A validated, compiled gate list for one qubit count and precision."""
+
+    def __init__(self, num_qubits, precision, gates, theta=None, fusion=FUSION_NONE, max_block_qubits=0,
+                 use_tensor_cores=0):
+        gates = np.ascontiguousarray(gates, dtype=GATE_DTYPE)
+        self.h = ctypes.c_void_p()
+        opts = _options(fusion, max_block_qubits, use_tensor_cores)
+        tp, tn, self._keep = _theta_arg(theta)
+        check(lib.qi_plan_create(int(num_qubits), int(precision), gates.ctypes.data if gates.size else None,
+                                 gates.size, tp, tn, ctypes.byref(opts), ctypes.byref(self.h)))
+
+    def execute(self, state):
+        check(lib.qi_plan_execute(self.h, state.h))
+
+    def stats(self):
+        s = _abi.PlanStats()
+        check(lib.qi_plan_stats_get(self.h, ctypes.byref(s)))
+        return {"n_gates": s.n_gates, "n_kernels": s.n_kernels, "n_blocks_by_k": list(s.n_blocks_by_k),
+                "predicted_us": s.predicted_us}
+
+    def ops(self):
+        """The plan's device operations: list of dicts (kind, k, targets, control_mask,
+        xmask, zmask, matrix as complex numpy array)."""
+        n = ctypes.c_int64()
+        check(lib.qi_plan_num_ops(self.h, ctypes.byref(n)))
+        out = []
+        for i in range(n.value):
+            info = _abi.PlanOpInfo()
+            check(lib.qi_plan_op_get(self.h, i, ctypes.byref(info), None, 0))
+            buf = np.zeros(2 * max(1, info.n_matrix), dtype=np.float64)
+            check(lib.qi_plan_op_get(self.h, i, ctypes.byref(info), buf.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                     info.n_matrix))
+            mat = buf[0::2][:info.n_matrix] + 1j * buf[1::2][:info.n_matrix]
+            out.append({"kind": info.kind, "k": info.k, "targets": list(info.targets)[:max(info.k, 0)],
+                        "control_mask": info.control_mask, "xmask": info.xmask, "zmask": info.zmask,
+                        "matrix": mat})
+        return out
+
+    def close(self):
+        if self.h:
+            lib.qi_plan_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def circuit_execute(state, gates, theta=None, fusion=FUSION_NONE, max_block_qubits=0, use_tensor_cores=0):
+    """Circuit::execute (src/circuit.rs:160-172) on a resident state (in place)."""
+    gates = np.ascontiguousarray(gates, dtype=GATE_DTYPE)
+    opts = _options(fusion, max_block_qubits, use_tensor_cores)
+    tp, tn, _keep = _theta_arg(theta)
+    check(lib.qi_circuit_execute(state.h, gates.ctypes.data if gates.size else None, gates.size, tp, tn,
+                                 ctypes.byref(opts)))
+
+
+def _terms(terms):
+    return np.ascontiguousarray(terms, dtype=TERM_DTYPE)
+
+
+def sumop_expectation(state, terms):
+    t = _terms(terms)
+    out = (ctypes.c_double * 2)()
+    check(lib.qi_sumop_expectation(state.h, t.ctypes.data if t.size else None, t.size, out))
+    return complex(out[0], out[1])
+
+
+def sumop_apply(out_state, in_state, terms):
+    t = _terms(terms)
+    check(lib.qi_sumop_apply(out_state.h, in_state.h, t.ctypes.data if t.size else None, t.size))
+
+
+def pauli_apply(out_state, in_state, term_row):
+    t = _terms(term_row).reshape(())
+    check(lib.qi_pauli_apply(out_state.h, in_state.h, t.ctypes.data))
+
+
+def pauli_apply_normalised(state, term_row):
+    t = _terms(term_row).reshape(())
+    check(lib.qi_pauli_apply_normalised(state.h, t.ctypes.data))
+
+
+def pauli_apply_exp(state, term_row):
+    t = _terms(term_row).reshape(())
+    check(lib.qi_pauli_apply_exp(state.h, t.ctypes.data))
+
+
+def pauli_apply_exp_factor(state, term_row, factor):
+    t = _terms(term_row).reshape(())
+    f = complex(factor)
+    check(lib.qi_pauli_apply_exp_factor(state.h, t.ctypes.data, f.real, f.imag))
+
+
+def pauli_apply_exp_neg_i_dt(state, term_row, dt):
+    t = _terms(term_row).reshape(())
+    check(lib.qi_pauli_apply_exp_neg_i_dt(state.h, t.ctypes.data, float(dt)))
+
+
+def trotter_evolve(state, terms, dt, num_steps, order=1, observable=None, observe_every=0):
+    """trotter_evolve_state (src/algorithms/time_evolution.rs:140-166); returns the
+    list of <observable> values taken every `observe_every` steps."""
+    t = _terms(terms)
+    nobs = 0
+    obs_ptr = None
+    energies = None
+    if observable is not None and observe_every > 0:
+        o = _terms(observable)
+        obs_ptr = o.ctypes.data
+        nobs = o.size
+        energies = np.zeros(2 * max(1, num_steps // observe_every), dtype=np.float64)
+    check(lib.qi_trotter_evolve(state.h, t.ctypes.data if t.size else None, t.size, float(dt), int(num_steps),
+                                int(order), obs_ptr, nobs, int(observe_every),
+                                energies.ctypes.data_as(ctypes.POINTER(ctypes.c_double)) if energies is not None
+                                else None))
+    if energies is None:
+        return []
+    return [complex(energies[2 * k], energies[2 * k + 1]) for k in range(num_steps // observe_every)]
+
+
+KERNEL_OF_OP_KIND = {1: "k_mat1", 2: "k_swap", 3: "k_mat2", 4: "k_fused", 5: "k_pauli_exp", 6: "k_pauli_exp+normalise",
+                     7: "k_diagk"}
+
+
+def plan_profile(plan, state):
+    """Run `plan` once on `state` with CUDA events around every op (on the state's
+    stream); returns (ops, per-op milliseconds)."""
+    ops = plan.ops()
+    ms = (ctypes.c_float * max(1, len(ops)))()
+    check(lib.qi_plan_profile(plan.h, state.h, ms))
+    return ops, [float(ms[i]) for i in range(len(ops))]

@@ -1,0 +1,176 @@
+"""ctypes binding of the engine's C ABI (include/qi_engine.h).
+
+Loads quant-iron_gb300/lib/libqi_gb300.so.  There is no fallback: if the
+library is missing the import fails with an error that says how to build it.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "lib", "libqi_gb300.so")
+
+if not os.path.exists(LIB_PATH):
+    raise ImportError("quant-iron GB300 engine library not found at %s; build it with "
+                      "`python -c 'import __graft_entry__ as g; g.build()'`" % LIB_PATH)
+lib = ctypes.CDLL(LIB_PATH)
+
+# ---------------------------------------------------------------- constants
+OK = 0
+F64 = 0
+F32 = 1
+FUSION_NONE = 0
+FUSION_GREEDY = 1
+FUSION_LEARNED = 2
+MAX_CONTROLS = 32
+
+# qi_status -> name of the quant_iron::errors::Error variant (src/errors.rs:4-97)
+STATUS_NAMES = {
+    -1: "InvalidNumberOfMeasurements",
+    -2: "OverlappingControlAndTargetQubits",
+    -3: "InvalidNumberOfQubits",
+    -4: "InvalidQubitIndex",
+    -5: "StateVectorNotNormalised",
+    -6: "NonUnitaryMatrix",
+    -7: "InvalidNumberOfInputs",
+    -8: "MismatchedNumberOfParameters",
+    -9: "UnknownError",
+    -10: "OpenCLError",
+    -11: "GpuContextLockError",
+    -12: "CircuitMacroError",
+    -13: "InvalidInputValue",
+    -14: "ZeroNorm",
+    -15: "InvalidPauliStringCoefficient",
+    -16: "OutOfMemory",
+    -17: "Timeout",
+    -18: "NullArgument",
+    -19: "Unsupported",
+}
+
+GATE_KINDS = dict(H=0, X=1, Y=2, Z=3, S=4, T=5, SDAG=6, TDAG=7, P=8, RX=9, RY=10, RZ=11, U2=12, RYPHASE=13,
+                  RYPHASE_DAG=14, CNOT=15, SWAP=16, MATCHGATE=17, TOFFOLI=18, IDENTITY=19, PAULI_STRING=20,
+                  PAULI_EVOLUTION=21)
+
+# qi_gate as a numpy structured dtype (same layout as the C struct)
+GATE_DTYPE = np.dtype([
+    ("kind", "<i4"), ("n_targets", "<i4"), ("n_controls", "<i4"), ("param_ids", "<i4", (3,)),
+    ("targets", "<i4", (2,)), ("controls", "<i4", (MAX_CONTROLS,)), ("params", "<f8", (8,)),
+    ("xmask", "<u8"), ("zmask", "<u8"),
+], align=True)
+assert GATE_DTYPE.itemsize == 240, GATE_DTYPE.itemsize
+
+TERM_DTYPE = np.dtype([("re", "<f8"), ("im", "<f8"), ("xmask", "<u8"), ("zmask", "<u8")])
+
+
+class ErrorInfo(ctypes.Structure):
+    _fields_ = [("code", ctypes.c_int32), ("reserved", ctypes.c_int32), ("a", ctypes.c_int64),
+                ("b", ctypes.c_int64), ("re", ctypes.c_double), ("im", ctypes.c_double),
+                ("message", ctypes.c_char * 256)]
+
+
+class ExecOptions(ctypes.Structure):
+    _fields_ = [("fusion", ctypes.c_int32), ("max_block_qubits", ctypes.c_int32),
+                ("use_tensor_cores", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+
+
+class PlanStats(ctypes.Structure):
+    _fields_ = [("n_gates", ctypes.c_int64), ("n_kernels", ctypes.c_int64), ("n_blocks_by_k", ctypes.c_int64 * 7),
+                ("predicted_us", ctypes.c_double)]
+
+
+class PlanOpInfo(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int32), ("k", ctypes.c_int32), ("targets", ctypes.c_int32 * 6),
+                ("control_mask", ctypes.c_uint64), ("xmask", ctypes.c_uint64), ("zmask", ctypes.c_uint64),
+                ("n_matrix", ctypes.c_int64)]
+
+
+_vp = ctypes.c_void_p
+_i32 = ctypes.c_int32
+_i64 = ctypes.c_int64
+_u64 = ctypes.c_uint64
+_d = ctypes.c_double
+_pd = ctypes.POINTER(ctypes.c_double)
+
+SIGNATURES = {
+    "qi_last_error": (_i32, [ctypes.POINTER(ErrorInfo)]),
+    "qi_version": (ctypes.c_char_p, []),
+    "qi_launch_count": (_u64, []),
+    "qi_set_device": (_i32, [_i32]),
+    "qi_state_create": (_i32, [_i32, _i32, ctypes.POINTER(_vp)]),
+    "qi_state_destroy": (_i32, [_vp]),
+    "qi_state_info": (_i32, [_vp, ctypes.POINTER(_i32), ctypes.POINTER(_i32)]),
+    "qi_state_set_stream": (_i32, [_vp, _vp]),
+    "qi_state_get_stream": (_i32, [_vp, ctypes.POINTER(_vp)]),
+    "qi_state_device_ptr": (_i32, [_vp, ctypes.POINTER(_vp)]),
+    "qi_state_synchronize": (_i32, [_vp]),
+    "qi_state_upload": (_i32, [_vp, _vp, _u64]),
+    "qi_state_download": (_i32, [_vp, _vp, _u64]),
+    "qi_state_set_zero": (_i32, [_vp]),
+    "qi_state_set_basis": (_i32, [_vp, _u64]),
+    "qi_state_set_plus": (_i32, [_vp]),
+    "qi_state_set_minus": (_i32, [_vp]),
+    "qi_state_set_ghz": (_i32, [_vp]),
+    "qi_state_check_normalised": (_i32, [_vp]),
+    "qi_state_copy": (_i32, [_vp, _vp]),
+    "qi_state_scale": (_i32, [_vp, _d, _d]),
+    "qi_state_axpy": (_i32, [_vp, _d, _d, _vp]),
+    "qi_state_inner_product": (_i32, [_vp, _vp, _pd]),
+    "qi_state_norm_sqr": (_i32, [_vp, _pd]),
+    "qi_state_normalise": (_i32, [_vp]),
+    "qi_state_tensor_product": (_i32, [_vp, _vp, _vp]),
+    "qi_state_amplitude": (_i32, [_vp, _u64, _pd]),
+    "qi_apply_gate": (_i32, [_vp, _vp]),
+    "qi_unitary2_check": (_i32, [_pd]),
+    "qi_pauli_apply": (_i32, [_vp, _vp, _vp]),
+    "qi_pauli_apply_normalised": (_i32, [_vp, _vp]),
+    "qi_pauli_apply_exp": (_i32, [_vp, _vp]),
+    "qi_pauli_apply_exp_factor": (_i32, [_vp, _vp, _d, _d]),
+    "qi_pauli_apply_exp_neg_i_dt": (_i32, [_vp, _vp, _d]),
+    "qi_sumop_apply": (_i32, [_vp, _vp, _vp, _i64]),
+    "qi_sumop_expectation": (_i32, [_vp, _vp, _i64, _pd]),
+    "qi_trotter_evolve": (_i32, [_vp, _vp, _i64, _d, _i64, _i32, _vp, _i64, _i64, _pd]),
+    "qi_plan_create": (_i32, [_i32, _i32, _vp, _i64, _pd, _i64, ctypes.POINTER(ExecOptions), ctypes.POINTER(_vp)]),
+    "qi_plan_execute": (_i32, [_vp, _vp]),
+    "qi_plan_stats_get": (_i32, [_vp, ctypes.POINTER(PlanStats)]),
+    "qi_plan_destroy": (_i32, [_vp]),
+    "qi_plan_num_ops": (_i32, [_vp, ctypes.POINTER(_i64)]),
+    "qi_plan_op_get": (_i32, [_vp, _i64, ctypes.POINTER(PlanOpInfo), _pd, _i64]),
+    "qi_circuit_execute": (_i32, [_vp, _vp, _i64, _pd, _i64, ctypes.POINTER(ExecOptions)]),
+}
+
+for _name, (_res, _args) in SIGNATURES.items():
+    _fn = getattr(lib, _name)
+    _fn.restype = _res
+    _fn.argtypes = _args
+
+
+class QuantIronError(Exception):
+    """A failed engine call: `variant` names the quant_iron::errors::Error variant,
+    `args_` holds its tuple fields."""
+
+    def __init__(self, code, a=-1, b=-1, message="", re=0.0, im=0.0):
+        self.code = code
+        self.variant = STATUS_NAMES.get(code, "Unknown(%d)" % code)
+        self.a, self.b = a, b
+        self.coeff = complex(re, im)
+        self.message = message
+        super().__init__("%s(%s)%s" % (self.variant, ", ".join(str(x) for x in (a, b) if x != -1),
+                                       (": " + message) if message else ""))
+
+
+def last_error():
+    info = ErrorInfo()
+    lib.qi_last_error(ctypes.byref(info))
+    return info
+
+
+def check(status):
+    if status != OK:
+        info = last_error()
+        raise QuantIronError(status, info.a, info.b, info.message.decode(errors="replace"), info.re, info.im)
+    return status
+
+
+lib.qi_plan_profile.restype = _i32
+lib.qi_plan_profile.argtypes = [_vp, _vp, ctypes.POINTER(ctypes.c_float)]

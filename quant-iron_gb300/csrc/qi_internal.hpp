@@ -1,0 +1,143 @@
+// qi_internal.hpp — declarations shared by the engine's translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <atomic>
+#include <cstdint>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/qi_engine.h"
+
+namespace qi {
+
+// ---------------------------------------------------------------- errors --
+struct Status {
+    qi_status code = QI_OK;
+    int64_t a = -1, b = -1;
+    double re = 0.0, im = 0.0;
+    std::string msg;
+    bool ok() const { return code == QI_OK; }
+};
+inline Status ok_status() { return Status{}; }
+inline Status err(qi_status c, int64_t a = -1, int64_t b = -1, std::string m = std::string()) {
+    Status s;
+    s.code = c; s.a = a; s.b = b; s.msg = std::move(m);
+    return s;
+}
+// Record `s` as the calling thread's last error and return its code.
+qi_status publish(const Status &s);
+Status cuda_status(cudaError_t e, const char *what);
+
+#define QI_CUDA(call)                                                   \
+    do {                                                                \
+        cudaError_t qi_e_ = (call);                                     \
+        if (qi_e_ != cudaSuccess) return ::qi::cuda_status(qi_e_, #call); \
+    } while (0)
+
+// Counts every kernel launch made by the engine (reported by the benchmark).
+extern std::atomic<uint64_t> g_launches;
+inline void count_launch(uint64_t k = 1) { g_launches.fetch_add(k, std::memory_order_relaxed); }
+Status check_launch(const char *what);
+
+// ----------------------------------------------------------------- state --
+constexpr int kReduceBlocks = 1216;  // 152 SMs x 8: partial-sum slots per reduction
+constexpr int kReduceThreads = 256;
+
+}  // namespace qi
+
+// Device-resident state vector handle (the opaque qi_state of the C ABI).
+struct qi_state {
+    int32_t n = 0;
+    int32_t prec = QI_F64;
+    int32_t device = 0;
+    void *amps = nullptr;             // 2^n complex amplitudes (double2 or float2)
+    cudaStream_t own_stream = nullptr;
+    cudaStream_t stream = nullptr;    // stream all work of this handle is issued on
+    std::recursive_mutex mu;          // serialises calls on this handle
+    double *d_partials = nullptr;     // reduction scratch: kReduceBlocks x 4 doubles
+    double *d_result = nullptr;       // finalised reduction results (8 doubles)
+    double *h_result = nullptr;       // pinned mirror of d_result
+    void *d_staging = nullptr;        // host<->device conversion staging (lazy)
+    size_t staging_bytes = 0;
+    int *d_flag = nullptr;            // device-side error flag (ZeroNorm inside async sequences)
+
+    uint64_t dim() const { return 1ull << n; }
+    size_t amp_bytes() const { return prec == QI_F64 ? 16 : 8; }
+    size_t bytes() const { return dim() * amp_bytes(); }
+};
+
+namespace qi {
+
+// --------------------------------------------------------- state helpers --
+Status state_reduce_norm_sqr(qi_state *s, double *out);                       // sync
+Status state_inner(qi_state *a, qi_state *b, double out[2]);                  // sync
+Status state_scale_async(qi_state *s, double re, double im);
+Status state_normalise_device_async(qi_state *s);   // norm on device, divides if != 0 and != 1; flags ZeroNorm
+Status state_read_flag(qi_state *s, int *flag);      // sync; resets the flag
+Status state_copy_async(qi_state *dst, const qi_state *src);
+
+// ----------------------------------------------------------------- gates --
+// A gate lowered to one primitive device operation.
+enum OpKind : int32_t {
+    OP_NOP = 0,
+    OP_MAT1 = 1,    // 2x2 on one target, controlled
+    OP_SWAP = 2,    // swap |..1..0..> <-> |..0..1..> on (t0, t1), controlled
+    OP_MAT2 = 3,    // 4x4 on (t0 < t1), controlled
+    OP_FUSED = 4,   // dense 2^k x 2^k on k targets (fused block)
+    OP_PAULI_EXP = 5,     // cosh(a) psi + sinh(a) P psi
+    OP_PAULI_NORM = 6,    // P psi then normalise (Gate::PauliString)
+    OP_DIAGK = 7,         // diagonal on k targets (2^k phases), controlled by nothing
+};
+enum Mat1Mode : int32_t { M1_GENERAL = 0, M1_DIAG = 1, M1_ANTIDIAG = 2, M1_PHASE1 = 3, M1_REAL = 4 };
+
+struct Op {
+    int32_t kind = OP_NOP;
+    int32_t mode = 0;
+    int32_t k = 0;                 // number of targets
+    int32_t targets[6] = {0, 0, 0, 0, 0, 0};
+    uint64_t cmask = 0;            // control mask (controls must be 1)
+    double m[32] = {0};            // MAT1: 4 complex; MAT2: 16 complex (row-major re, im)
+    int64_t mat_offset = -1;       // OP_FUSED / OP_DIAGK: offset (complex entries) into the plan's matrix buffer
+    uint64_t xmask = 0, zmask = 0; // Pauli ops
+    double alpha_re = 0, alpha_im = 0;   // Pauli exp: cosh/sinh coefficients are derived from this
+    double cre = 0, cim = 0, sre = 0, sim = 0;
+};
+
+// Host-side description of a gate after validation: 2x2 / 4x4 matrix on its
+// targets plus controls.  Used by both the per-gate lowering and the fuser.
+struct GateMatrix {
+    int32_t kind = -1;             // qi_gate_kind
+    int32_t nt = 0;                // 0 = identity (no-op), 1 or 2 targets
+    int32_t t[2] = {0, 0};         // targets (for nt == 2: t[0] < t[1] after normalisation)
+    std::vector<int32_t> controls; // deduplicated
+    double m[32];                  // row-major complex (re, im) 2^nt x 2^nt
+    bool diagonal = false;
+    bool pauli = false;            // Gate::PauliString / PauliTimeEvolution (not fusable as a matrix)
+    bool normalise_after = false;
+    uint64_t xmask = 0, zmask = 0;
+    double alpha_re = 0, alpha_im = 0;
+};
+
+Status validate_gate(int n, const qi_gate &g);
+// Validate + build the matrix of a (resolved) gate.
+Status gate_to_matrix(int n, const qi_gate &g, GateMatrix *out);
+// Lower a GateMatrix to a single primitive op.
+Op lower_gate(int n, const GateMatrix &gm);
+// Launch one primitive op on the state's stream (no synchronisation).
+Status launch_op(qi_state *s, const Op &op, const void *d_mats);
+
+// ------------------------------------------------------------------ pauli --
+Status launch_pauli_exp(qi_state *s, uint64_t xmask, uint64_t zmask, double cre, double cim, double sre, double sim);
+Status launch_pauli_apply(qi_state *out, qi_state *in, uint64_t xmask, uint64_t zmask, double cre, double cim);
+Status validate_pauli(int n, const qi_pauli_term &t);
+
+// ------------------------------------------------------------------ fused --
+// Apply a dense 2^k x 2^k complex matrix (device pointer, row-major, element
+// type matches the state's precision) on sorted targets.
+Status launch_fused(qi_state *s, int k, const int32_t *targets, const void *d_mat, int use_tc);
+Status launch_diagk(qi_state *s, int k, const int32_t *targets, const void *d_phases);
+
+}  // namespace qi

@@ -1,0 +1,497 @@
+// qi_pauli.cu — Pauli-string kernels: exp(alpha P) in one pass, P|psi>,
+// SumOp apply and SumOp expectation grouped by X-mask, Trotter evolution.
+//
+// Reference: src/components/pauli_string.rs (apply :139-151, apply_exp_factor
+// :237-262, SumOp::apply :453-466, expectation_value :485-507) and
+// src/algorithms/time_evolution.rs:45-166.
+//
+// For a Pauli string with X-or-Y qubits xmask, Z-or-Y qubits zmask and ny Y
+// factors, (P psi)_i = (-i)^ny (-1)^popcount(i & zmask) psi_{i ^ xmask}.
+// The reference applies each single-qubit Pauli as a full pass and builds
+// cosh(a) psi + sinh(a) P psi from three state vectors; here one pass reads
+// the pair (i, i ^ xmask) and writes both outputs.
+#include "qi_internal.hpp"
+#include "qi_device.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <map>
+
+namespace qi {
+
+// (-i)^ny as (re, im)
+static inline void minus_i_pow(int ny, double &re, double &im) {
+    switch (ny & 3) {
+    case 0: re = 1; im = 0; break;
+    case 1: re = 0; im = -1; break;
+    case 2: re = -1; im = 0; break;
+    default: re = 0; im = 1; break;
+    }
+}
+
+struct ExpParams {
+    uint64_t nwork;
+    uint64_t xmask, zmask;
+    uint64_t hbit;     // highest bit of xmask (pair enumeration), 0 if xmask == 0
+    int32_t hpos;
+    int32_t swap_halves;   // VEC: xmask bit 0 set -> partner float4 halves are swapped
+    double cre, cim;   // cosh(alpha)
+    double sre, sim;   // sinh(alpha) * (-i)^ny
+};
+
+// Diagonal case (xmask == 0): psi_i *= cosh + sinh * (-1)^popc(i & z).
+template <typename T>
+__global__ void __launch_bounds__(256) k_pauli_exp_diag(typename Cx<T>::V2 *a, ExpParams p) {
+    using X = Cx<T>;
+    const typename X::V2 plus = X::make((T)(p.cre + p.sre), (T)(p.cim + p.sim));
+    const typename X::V2 minus = X::make((T)(p.cre - p.sre), (T)(p.cim - p.sim));
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < p.nwork; i += stride) {
+        typename X::V2 v = a[i];
+        a[i] = X::mul((__popcll(i & p.zmask) & 1) ? minus : plus, v);
+    }
+}
+
+// Pair case: i with bit hpos clear, j = i ^ xmask.
+//   new_i = c psi_i + s (-1)^popc(i&z) psi_j,  new_j = c psi_j + s (-1)^popc(j&z) psi_i
+template <typename T, bool VEC>
+__global__ void __launch_bounds__(256) k_pauli_exp_pair(typename Cx<T>::V2 *a, ExpParams p) {
+    using X = Cx<T>;
+    const typename X::V2 c = X::make((T)p.cre, (T)p.cim);
+    const typename X::V2 s = X::make((T)p.sre, (T)p.sim);
+    const typename X::V2 sn = X::make((T)-p.sre, (T)-p.sim);
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    const uint64_t lo_mask = p.hbit - 1;
+    for (uint64_t w = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; w < p.nwork; w += stride) {
+        const uint64_t ww = VEC ? (w << 1) : w;
+        const uint64_t i = ((ww & ~lo_mask) << 1) | (ww & lo_mask);
+        const uint64_t j = i ^ p.xmask;
+        if constexpr (VEC) {
+            // i even; the partner pair (j, j^1) lives in float4 j >> 1
+            float4 *a4 = reinterpret_cast<float4 *>(a);
+            float4 u = a4[i >> 1], v = a4[j >> 1];
+            float2 i0 = make_float2(u.x, u.y), i1 = make_float2(u.z, u.w);
+            float2 j0 = make_float2(v.x, v.y), j1 = make_float2(v.z, v.w);
+            if (p.swap_halves) { float2 t = j0; j0 = j1; j1 = t; }   // j0 = psi_{i ^ x}, j1 = psi_{(i+1) ^ x}
+            const uint64_t ja = j, jb = j ^ 1ull;   // partners of i and i+1
+            float2 ni0 = X::fma((__popcll(i & p.zmask) & 1) ? sn : s, j0, X::mul(c, i0));
+            float2 ni1 = X::fma((__popcll((i + 1) & p.zmask) & 1) ? sn : s, j1, X::mul(c, i1));
+            float2 nj0 = X::fma((__popcll(ja & p.zmask) & 1) ? sn : s, i0, X::mul(c, j0));
+            float2 nj1 = X::fma((__popcll(jb & p.zmask) & 1) ? sn : s, i1, X::mul(c, j1));
+            if (p.swap_halves) { float2 t = nj0; nj0 = nj1; nj1 = t; }
+            a4[i >> 1] = make_float4(ni0.x, ni0.y, ni1.x, ni1.y);
+            a4[j >> 1] = make_float4(nj0.x, nj0.y, nj1.x, nj1.y);
+        } else {
+            typename X::V2 x = a[i], y = a[j];
+            a[i] = X::fma((__popcll(i & p.zmask) & 1) ? sn : s, y, X::mul(c, x));
+            a[j] = X::fma((__popcll(j & p.zmask) & 1) ? sn : s, x, X::mul(c, y));
+        }
+    }
+}
+
+// out_i = coeff * (-i)^ny (-1)^popc(i&z) in_{i ^ x}   (PauliString::apply, out of place)
+template <typename T>
+__global__ void __launch_bounds__(256) k_pauli_gather(typename Cx<T>::V2 *o, const typename Cx<T>::V2 *in, uint64_t dim,
+                                                      uint64_t xmask, uint64_t zmask, double fre, double fim) {
+    using X = Cx<T>;
+    const typename X::V2 f = X::make((T)fre, (T)fim), fn = X::make((T)-fre, (T)-fim);
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < dim; i += stride)
+        o[i] = X::mul((__popcll(i & zmask) & 1) ? fn : f, in[i ^ xmask]);
+}
+
+static unsigned pgrid(uint64_t work) {
+    uint64_t g = (work + 255) / 256;
+    if (g < 1) g = 1;
+    if (g > 152 * 8) g = 152 * 8;
+    return (unsigned)g;
+}
+
+Status launch_pauli_exp(qi_state *s, uint64_t xmask, uint64_t zmask, double cre, double cim, double sre, double sim) {
+    ExpParams p;
+    std::memset(&p, 0, sizeof(p));
+    p.xmask = xmask;
+    p.zmask = zmask;
+    double pr, pi;
+    minus_i_pow(__builtin_popcountll(xmask & zmask), pr, pi);
+    p.cre = cre; p.cim = cim;
+    p.sre = sre * pr - sim * pi;
+    p.sim = sre * pi + sim * pr;
+    const bool f32 = s->prec == QI_F32;
+    if (xmask == 0) {
+        p.nwork = s->dim();
+        unsigned g = pgrid(p.nwork);
+        if (f32) k_pauli_exp_diag<float><<<g, 256, 0, s->stream>>>((float2 *)s->amps, p);
+        else k_pauli_exp_diag<double><<<g, 256, 0, s->stream>>>((double2 *)s->amps, p);
+        count_launch();
+        return check_launch("k_pauli_exp_diag");
+    }
+    int h = 63 - __builtin_clzll(xmask);
+    p.hpos = h;
+    p.hbit = 1ull << h;
+    const bool vec = f32 && h >= 1 && s->n >= 2;
+    p.swap_halves = (xmask & 1ull) ? 1 : 0;
+    p.nwork = s->dim() >> (vec ? 2 : 1);
+    unsigned g = pgrid(p.nwork);
+    if (f32) {
+        if (vec) k_pauli_exp_pair<float, true><<<g, 256, 0, s->stream>>>((float2 *)s->amps, p);
+        else k_pauli_exp_pair<float, false><<<g, 256, 0, s->stream>>>((float2 *)s->amps, p);
+    } else {
+        k_pauli_exp_pair<double, false><<<g, 256, 0, s->stream>>>((double2 *)s->amps, p);
+    }
+    count_launch();
+    return check_launch("k_pauli_exp_pair");
+}
+
+Status launch_pauli_apply(qi_state *out, qi_state *in, uint64_t xmask, uint64_t zmask, double cre, double cim) {
+    double pr, pi;
+    minus_i_pow(__builtin_popcountll(xmask & zmask), pr, pi);
+    const double fre = cre * pr - cim * pi, fim = cre * pi + cim * pr;
+    unsigned g = pgrid(out->dim());
+    if (out->prec == QI_F32)
+        k_pauli_gather<float><<<g, 256, 0, out->stream>>>((float2 *)out->amps, (const float2 *)in->amps, out->dim(),
+                                                          xmask, zmask, fre, fim);
+    else
+        k_pauli_gather<double><<<g, 256, 0, out->stream>>>((double2 *)out->amps, (const double2 *)in->amps, out->dim(),
+                                                           xmask, zmask, fre, fim);
+    count_launch();
+    return check_launch("k_pauli_gather");
+}
+
+// ------------------------------------------------- grouped SumOp kernels --
+// Terms are grouped by xmask.  For group g with xmask x:
+//   f_g(i) = sum_{k in g} c_k (-i)^{ny_k} (-1)^popc(i & z_k)
+//   (H psi)_i = sum_g f_g(i) psi_{i ^ x_g}
+//   <psi|H|psi> = sum_g sum_i conj(psi_i) f_g(i) psi_{i ^ x_g}
+struct GroupTerm {
+    uint64_t zmask;
+    double re, im;   // c_k (-i)^{ny_k}
+};
+struct GroupHdr {
+    uint64_t xmask;
+    int32_t first, count;   // into the term array
+};
+
+struct SumOpDev {
+    GroupHdr *groups = nullptr;
+    GroupTerm *terms = nullptr;
+    int ngroups = 0;
+    int nterms = 0;
+    size_t cap_groups = 0, cap_terms = 0;
+};
+
+template <typename T>
+__device__ __forceinline__ typename Cx<T>::V2 group_factor(const GroupTerm *t, int cnt, uint64_t i) {
+    T re = 0, im = 0;
+    for (int k = 0; k < cnt; ++k) {
+        const GroupTerm g = t[k];
+        const T sgn = (__popcll(i & g.zmask) & 1) ? T(-1) : T(1);
+        re += sgn * (T)g.re;
+        im += sgn * (T)g.im;
+    }
+    return Cx<T>::make(re, im);
+}
+
+// Expectation contribution of one group, FP64 block partials.
+template <typename T>
+__global__ void __launch_bounds__(256) k_group_expect(const typename Cx<T>::V2 *a, uint64_t dim, GroupHdr hdr,
+                                                       const GroupTerm *terms, double *partials) {
+    using X = Cx<T>;
+    extern __shared__ GroupTerm sterm[];
+    for (int k = threadIdx.x; k < hdr.count; k += blockDim.x) sterm[k] = terms[hdr.first + k];
+    __syncthreads();
+    double re = 0.0, im = 0.0;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    if (hdr.xmask == 0) {
+        for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < dim; i += stride) {
+            typename X::V2 v = ldg_stream(a + i);
+            const T p = v.x * v.x + v.y * v.y;
+            typename X::V2 f = group_factor<T>(sterm, hdr.count, i);
+            re += (double)(p * f.x);
+            im += (double)(p * f.y);
+        }
+    } else {
+        const int h = 63 - __clzll(hdr.xmask);
+        const uint64_t lo_mask = (1ull << h) - 1;
+        const uint64_t npairs = dim >> 1;
+        for (uint64_t w = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; w < npairs; w += stride) {
+            const uint64_t i = ((w & ~lo_mask) << 1) | (w & lo_mask);
+            const uint64_t j = i ^ hdr.xmask;
+            typename X::V2 x = a[i], y = a[j];
+            typename X::V2 fi = group_factor<T>(sterm, hdr.count, i);
+            typename X::V2 fj = group_factor<T>(sterm, hdr.count, j);
+            // conj(x) * fi * y + conj(y) * fj * x
+            typename X::V2 cxy = X::make(x.x * y.x + x.y * y.y, x.x * y.y - x.y * y.x);   // conj(x) y
+            typename X::V2 t0 = X::mul(fi, cxy);
+            typename X::V2 t1 = X::mul(fj, X::make(cxy.x, -cxy.y));                        // conj(y) x
+            re += (double)(t0.x + t1.x);
+            im += (double)(t0.y + t1.y);
+        }
+    }
+    double r0 = block_sum(re);
+    double r1 = block_sum(im);
+    if (threadIdx.x == 0) {
+        partials[blockIdx.x * 4 + 0] = r0;
+        partials[blockIdx.x * 4 + 1] = r1;
+    }
+}
+
+// acc[0..1] += fixed-order sum of the partials (one thread block).
+__global__ void k_accumulate(const double *partials, int nb, double *acc) {
+    for (int c = 0; c < 2; ++c) {
+        double v = 0.0;
+        for (int i = threadIdx.x; i < nb; i += blockDim.x) v += partials[i * 4 + c];
+        double r = block_sum(v);
+        if (threadIdx.x == 0) acc[c] += r;
+        __syncthreads();
+    }
+}
+
+// (H psi)_i = sum_g f_g(i) psi_{i ^ x_g}   (SumOp::apply)
+template <typename T>
+__global__ void __launch_bounds__(256) k_sumop_apply(typename Cx<T>::V2 *o, const typename Cx<T>::V2 *in, uint64_t dim,
+                                                     const GroupHdr *groups, int ngroups, const GroupTerm *terms,
+                                                     int nterms) {
+    using X = Cx<T>;
+    extern __shared__ unsigned char smem_raw[];
+    GroupTerm *sterm = reinterpret_cast<GroupTerm *>(smem_raw);
+    GroupHdr *shdr = reinterpret_cast<GroupHdr *>(sterm + nterms);
+    for (int k = threadIdx.x; k < nterms; k += blockDim.x) sterm[k] = terms[k];
+    for (int k = threadIdx.x; k < ngroups; k += blockDim.x) shdr[k] = groups[k];
+    __syncthreads();
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < dim; i += stride) {
+        typename X::V2 acc = X::make(0, 0);
+        for (int g = 0; g < ngroups; ++g) {
+            const GroupHdr h = shdr[g];
+            typename X::V2 f = group_factor<T>(sterm + h.first, h.count, i);
+            acc = X::fma(f, in[i ^ h.xmask], acc);
+        }
+        o[i] = acc;
+    }
+}
+
+// Build the grouped representation of a term list (host).
+static void group_terms(const qi_pauli_term *terms, int64_t nt, std::vector<GroupHdr> &hdrs,
+                        std::vector<GroupTerm> &out) {
+    std::map<uint64_t, std::vector<GroupTerm>> by_x;
+    std::vector<uint64_t> order;
+    for (int64_t k = 0; k < nt; ++k) {
+        const qi_pauli_term &t = terms[k];
+        double pr, pi;
+        minus_i_pow(__builtin_popcountll(t.xmask & t.zmask), pr, pi);
+        GroupTerm g;
+        g.zmask = t.zmask;
+        g.re = t.coeff_re * pr - t.coeff_im * pi;
+        g.im = t.coeff_re * pi + t.coeff_im * pr;
+        if (!by_x.count(t.xmask)) order.push_back(t.xmask);
+        by_x[t.xmask].push_back(g);
+    }
+    hdrs.clear();
+    out.clear();
+    for (uint64_t x : order) {
+        GroupHdr h;
+        h.xmask = x;
+        h.first = (int32_t)out.size();
+        h.count = (int32_t)by_x[x].size();
+        for (auto &g : by_x[x]) out.push_back(g);
+        hdrs.push_back(h);
+    }
+}
+
+static Status upload_groups(qi_state *s, const std::vector<GroupHdr> &hdrs, const std::vector<GroupTerm> &terms,
+                            GroupHdr **d_hdr, GroupTerm **d_terms) {
+    QI_CUDA(cudaMallocAsync((void **)d_hdr, std::max<size_t>(1, hdrs.size()) * sizeof(GroupHdr), s->stream));
+    QI_CUDA(cudaMallocAsync((void **)d_terms, std::max<size_t>(1, terms.size()) * sizeof(GroupTerm), s->stream));
+    QI_CUDA(cudaMemcpyAsync(*d_hdr, hdrs.data(), hdrs.size() * sizeof(GroupHdr), cudaMemcpyHostToDevice, s->stream));
+    QI_CUDA(cudaMemcpyAsync(*d_terms, terms.data(), terms.size() * sizeof(GroupTerm), cudaMemcpyHostToDevice, s->stream));
+    // host vectors are pageable: the copies complete before cudaMemcpyAsync returns
+    return ok_status();
+}
+
+// <psi|H|psi> into out[2]; synchronises.
+Status sumop_expectation(qi_state *s, const qi_pauli_term *terms, int64_t nt, double out[2]) {
+    std::vector<GroupHdr> hdrs;
+    std::vector<GroupTerm> gts;
+    group_terms(terms, nt, hdrs, gts);
+    GroupHdr *d_hdr = nullptr;
+    GroupTerm *d_terms = nullptr;
+    Status st = upload_groups(s, hdrs, gts, &d_hdr, &d_terms);
+    if (!st.ok()) return st;
+    QI_CUDA(cudaMemsetAsync(s->d_result, 0, 2 * sizeof(double), s->stream));
+    const bool f32 = s->prec == QI_F32;
+    for (const GroupHdr &h : hdrs) {
+        const uint64_t work = h.xmask ? (s->dim() >> 1) : s->dim();
+        uint64_t nb64 = (work + kReduceThreads - 1) / kReduceThreads;
+        const unsigned nb = (unsigned)std::min<uint64_t>(std::max<uint64_t>(nb64, 1), kReduceBlocks);
+        const size_t sm = (size_t)h.count * sizeof(GroupTerm);
+        if (f32)
+            k_group_expect<float><<<nb, kReduceThreads, sm, s->stream>>>((const float2 *)s->amps, s->dim(), h, d_terms,
+                                                                         s->d_partials);
+        else
+            k_group_expect<double><<<nb, kReduceThreads, sm, s->stream>>>((const double2 *)s->amps, s->dim(), h, d_terms,
+                                                                          s->d_partials);
+        k_accumulate<<<1, 256, 0, s->stream>>>(s->d_partials, (int)nb, s->d_result);
+        count_launch(2);
+        st = check_launch("k_group_expect");
+        if (!st.ok()) return st;
+    }
+    QI_CUDA(cudaMemcpyAsync(s->h_result, s->d_result, 2 * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+    QI_CUDA(cudaFreeAsync(d_hdr, s->stream));
+    QI_CUDA(cudaFreeAsync(d_terms, s->stream));
+    QI_CUDA(cudaStreamSynchronize(s->stream));
+    out[0] = s->h_result[0];
+    out[1] = s->h_result[1];
+    return ok_status();
+}
+
+Status sumop_apply(qi_state *o, qi_state *in, const qi_pauli_term *terms, int64_t nt) {
+    std::vector<GroupHdr> hdrs;
+    std::vector<GroupTerm> gts;
+    group_terms(terms, nt, hdrs, gts);
+    GroupHdr *d_hdr = nullptr;
+    GroupTerm *d_terms = nullptr;
+    Status st = upload_groups(o, hdrs, gts, &d_hdr, &d_terms);
+    if (!st.ok()) return st;
+    const size_t sm = gts.size() * sizeof(GroupTerm) + hdrs.size() * sizeof(GroupHdr);
+    if (sm > 200 * 1024) return err(QI_ERR_UNSUPPORTED, (int64_t)nt, -1, "too many Pauli terms for one pass");
+    unsigned g = pgrid(o->dim());
+    if (o->prec == QI_F32) {
+        if (sm > 48 * 1024) QI_CUDA(cudaFuncSetAttribute(k_sumop_apply<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        k_sumop_apply<float><<<g, 256, sm, o->stream>>>((float2 *)o->amps, (const float2 *)in->amps, o->dim(), d_hdr,
+                                                       (int)hdrs.size(), d_terms, (int)gts.size());
+    } else {
+        if (sm > 48 * 1024) QI_CUDA(cudaFuncSetAttribute(k_sumop_apply<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        k_sumop_apply<double><<<g, 256, sm, o->stream>>>((double2 *)o->amps, (const double2 *)in->amps, o->dim(), d_hdr,
+                                                        (int)hdrs.size(), d_terms, (int)gts.size());
+    }
+    count_launch();
+    st = check_launch("k_sumop_apply");
+    if (!st.ok()) return st;
+    QI_CUDA(cudaFreeAsync(d_hdr, o->stream));
+    QI_CUDA(cudaFreeAsync(d_terms, o->stream));
+    return ok_status();
+}
+
+// cosh / sinh of a complex alpha with num_complex's formulas.
+void exp_coeffs(double ar, double ai, double &cre, double &cim, double &sre, double &sim) {
+    cre = std::cosh(ar) * std::cos(ai);
+    cim = std::sinh(ar) * std::sin(ai);
+    sre = std::sinh(ar) * std::cos(ai);
+    sim = std::cosh(ar) * std::sin(ai);
+}
+
+}  // namespace qi
+
+using namespace qi;
+
+#define QI_LOCK(s)                                                        \
+    if (!(s)) return publish(err(QI_ERR_NULL_ARGUMENT));                  \
+    std::lock_guard<std::recursive_mutex> qi_lk_((s)->mu);                \
+    {                                                                     \
+        cudaError_t qi_e_ = cudaSetDevice((s)->device);                   \
+        if (qi_e_ != cudaSuccess) return publish(cuda_status(qi_e_, "cudaSetDevice")); \
+    }
+
+extern "C" {
+
+qi_status qi_pauli_apply(qi_state *out, qi_state *in, const qi_pauli_term *t) {
+    QI_LOCK(out);
+    if (!in || !t) return publish(err(QI_ERR_NULL_ARGUMENT));
+    if (in->n != out->n) return publish(err(QI_ERR_INVALID_NUMBER_OF_QUBITS, in->n));
+    if (in->prec != out->prec) return publish(err(QI_ERR_UNSUPPORTED, -1, -1, "equal precisions required"));
+    Status st = validate_pauli(in->n, *t);
+    if (!st.ok()) return publish(st);
+    if (in == out) {
+        // in place: pair update with cosh = 0, sinh = coefficient
+        return publish(launch_pauli_exp(out, t->xmask, t->zmask, 0.0, 0.0, t->coeff_re, t->coeff_im));
+    }
+    if (in->stream != out->stream) {
+        cudaError_t e = cudaStreamSynchronize(in->stream);
+        if (e != cudaSuccess) return publish(cuda_status(e, "sync"));
+    }
+    return publish(launch_pauli_apply(out, in, t->xmask, t->zmask, t->coeff_re, t->coeff_im));
+}
+
+qi_status qi_pauli_apply_normalised(qi_state *s, const qi_pauli_term *t) {
+    QI_LOCK(s);
+    if (!t) return publish(err(QI_ERR_NULL_ARGUMENT));
+    Status st = validate_pauli(s->n, *t);
+    if (!st.ok()) return publish(st);
+    st = launch_pauli_exp(s, t->xmask, t->zmask, 0.0, 0.0, 1.0, 0.0);
+    if (!st.ok()) return publish(st);
+    st = state_normalise_device_async(s);
+    if (!st.ok()) return publish(st);
+    int flag = 0;
+    st = state_read_flag(s, &flag);
+    if (!st.ok()) return publish(st);
+    if (flag) return publish(err(QI_ERR_ZERO_NORM));
+    return publish(ok_status());
+}
+
+qi_status qi_pauli_apply_exp_factor(qi_state *s, const qi_pauli_term *t, double fre, double fim) {
+    QI_LOCK(s);
+    if (!t) return publish(err(QI_ERR_NULL_ARGUMENT));
+    Status st = validate_pauli(s->n, *t);
+    if (!st.ok()) return publish(st);
+    const double ar = t->coeff_re * fre - t->coeff_im * fim;   // alpha = coefficient * factor
+    const double ai = t->coeff_re * fim + t->coeff_im * fre;
+    if ((t->xmask | t->zmask) == 0) {   // identity string: state * exp(alpha)
+        const double e = std::exp(ar);
+        return publish(state_scale_async(s, e * std::cos(ai), e * std::sin(ai)));
+    }
+    double cre, cim, sre, sim;
+    exp_coeffs(ar, ai, cre, cim, sre, sim);
+    return publish(launch_pauli_exp(s, t->xmask, t->zmask, cre, cim, sre, sim));
+}
+
+qi_status qi_pauli_apply_exp(qi_state *s, const qi_pauli_term *t) {
+    return qi_pauli_apply_exp_factor(s, t, 1.0, 0.0);
+}
+
+qi_status qi_pauli_apply_exp_neg_i_dt(qi_state *s, const qi_pauli_term *t, double dt) {
+    if (!t) return publish(err(QI_ERR_NULL_ARGUMENT));
+    if (t->coeff_im != 0.0) {   // pauli_string.rs:282-284
+        Status e = err(QI_ERR_INVALID_PAULI_COEFFICIENT);
+        e.re = t->coeff_re;
+        e.im = t->coeff_im;
+        return publish(e);
+    }
+    return qi_pauli_apply_exp_factor(s, t, 0.0, -dt);
+}
+
+qi_status qi_sumop_apply(qi_state *out, qi_state *in, const qi_pauli_term *terms, int64_t n_terms) {
+    QI_LOCK(out);
+    if (!in || (!terms && n_terms > 0)) return publish(err(QI_ERR_NULL_ARGUMENT));
+    if (in->n != out->n) return publish(err(QI_ERR_INVALID_NUMBER_OF_QUBITS, in->n));
+    if (in->prec != out->prec) return publish(err(QI_ERR_UNSUPPORTED, -1, -1, "equal precisions required"));
+    if (in == out) return publish(err(QI_ERR_UNSUPPORTED, -1, -1, "SumOp::apply needs distinct input and output"));
+    for (int64_t k = 0; k < n_terms; ++k) {
+        Status st = validate_pauli(in->n, terms[k]);
+        if (!st.ok()) return publish(st);
+    }
+    if (in->stream != out->stream) {
+        cudaError_t e = cudaStreamSynchronize(in->stream);
+        if (e != cudaSuccess) return publish(cuda_status(e, "sync"));
+    }
+    if (n_terms == 0) {   // empty SumOp: state * 0.0 (pauli_string.rs:454-457)
+        Status st = state_copy_async(out, in);
+        if (!st.ok()) return publish(st);
+        return publish(state_scale_async(out, 0.0, 0.0));
+    }
+    return publish(sumop_apply(out, in, terms, n_terms));
+}
+
+qi_status qi_sumop_expectation(qi_state *s, const qi_pauli_term *terms, int64_t n_terms, double out[2]) {
+    QI_LOCK(s);
+    if (!out || (!terms && n_terms > 0)) return publish(err(QI_ERR_NULL_ARGUMENT));
+    out[0] = out[1] = 0.0;
+    if (n_terms == 0) return publish(ok_status());   // pauli_string.rs:486-489
+    for (int64_t k = 0; k < n_terms; ++k) {
+        Status st = validate_pauli(s->n, terms[k]);
+        if (!st.ok()) return publish(st);
+    }
+    return publish(sumop_expectation(s, terms, n_terms, out));
+}
+
+}  // extern "C"

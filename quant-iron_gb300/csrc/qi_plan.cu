@@ -1,0 +1,535 @@
+// qi_plan.cu — circuit plans: validation, the gate-fusion pass and execution.
+//
+// Reference: Circuit::execute (src/circuit.rs:160-172) applies gates one by
+// one, each a full copy of the state (Gate::apply, src/components/gate.rs:99-122).
+// A plan validates the whole gate list first (so an invalid gate leaves the
+// state untouched, as the reference's functional execute does), then lowers
+// it to device operations:
+//   QI_FUSION_NONE   one streaming kernel per gate (the plain per-gate method);
+//   QI_FUSION_GREEDY the greedy fuser below with block width k;
+//   QI_FUSION_LEARNED candidate partitions scored by the learned cost model
+//                    (qi_costmodel.cu), greedy as the fallback.
+//
+// Greedy fuser ("light-cone" absorption).  A block starts empty; the
+// remaining gates are scanned in order.  A gate joins the block when its
+// qubits fit (|Q u S| <= k) and it does not depend on a gate that was passed
+// over: passed-over gates block their qubits, except that diagonal gates
+// commute with each other, so a diagonal gate may pass over a diagonal gate.
+// Every absorbed gate therefore commutes with every passed-over gate it
+// overtakes, and the block can run before all of them.
+#include "qi_internal.hpp"
+#include "qi_plan.hpp"
+
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <thread>
+
+namespace qi {
+
+using cd = std::complex<double>;
+
+// ------------------------------------------------------------ elements ---
+static Elem make_elem_from_gate(const GateMatrix &gm, int src) {
+    Elem e;
+    e.src = src;
+    e.gm = gm;
+    if (gm.pauli) {
+        const uint64_t sup = gm.xmask | gm.zmask;
+        e.mask = gm.normalise_after ? ~0ull : sup;
+        e.diagonal = gm.xmask == 0 && !gm.normalise_after;
+        e.fusable = false;   // decided later (dense only if narrow enough)
+        e.pauli = true;
+        return e;
+    }
+    uint64_t m = 0;
+    for (int j = 0; j < gm.nt; ++j) m |= 1ull << gm.t[j];
+    for (int32_t c : gm.controls) m |= 1ull << c;
+    e.mask = m;
+    e.diagonal = gm.diagonal;
+    e.fusable = gm.nt > 0;
+    return e;
+}
+
+// Dense matrix of an element on its support (sorted qubits of e.mask).
+static void dense_of(const Elem &e, std::vector<int> &sup, std::vector<cd> &D) {
+    sup.clear();
+    for (int q = 0; q < 64; ++q)
+        if ((e.mask >> q) & 1ull) sup.push_back(q);
+    const int s = (int)sup.size();
+    const int dim = 1 << s;
+    D.assign((size_t)dim * dim, cd(0, 0));
+    auto local = [&](int q) { return (int)(std::find(sup.begin(), sup.end(), q) - sup.begin()); };
+    if (e.pauli) {
+        // cosh(a) I + sinh(a) P on the support
+        uint32_t lx = 0, lz = 0;
+        for (int j = 0; j < s; ++j) {
+            if ((e.gm.xmask >> sup[j]) & 1ull) lx |= 1u << j;
+            if ((e.gm.zmask >> sup[j]) & 1ull) lz |= 1u << j;
+        }
+        const int ny = __builtin_popcount(lx & lz);
+        const cd mi_pow[4] = {cd(1, 0), cd(0, -1), cd(-1, 0), cd(0, 1)};
+        const double ar = e.gm.alpha_re, ai = e.gm.alpha_im;
+        const cd ch(std::cosh(ar) * std::cos(ai), std::sinh(ar) * std::sin(ai));
+        const cd sh(std::sinh(ar) * std::cos(ai), std::cosh(ar) * std::sin(ai));
+        for (int o = 0; o < dim; ++o) {
+            D[(size_t)o * dim + o] += ch;
+            const double sg = (__builtin_popcount(o & lz) & 1) ? -1.0 : 1.0;
+            D[(size_t)o * dim + (o ^ lx)] += sh * mi_pow[ny & 3] * sg;
+        }
+        return;
+    }
+    const GateMatrix &g = e.gm;
+    uint32_t cmask = 0;
+    for (int32_t c : g.controls) cmask |= 1u << local(c);
+    int tl[2] = {0, 0};
+    for (int j = 0; j < g.nt; ++j) tl[j] = local(g.t[j]);
+    const int td = 1 << g.nt;
+    for (int col = 0; col < dim; ++col) {
+        if ((col & cmask) != cmask) { D[(size_t)col * dim + col] = cd(1, 0); continue; }
+        int tin = 0;
+        for (int j = 0; j < g.nt; ++j) tin |= ((col >> tl[j]) & 1) << j;
+        int rest = col;
+        for (int j = 0; j < g.nt; ++j) rest &= ~(1 << tl[j]);
+        for (int tout = 0; tout < td; ++tout) {
+            int row = rest;
+            for (int j = 0; j < g.nt; ++j) row |= ((tout >> j) & 1) << tl[j];
+            D[(size_t)row * dim + col] = cd(g.m[2 * (tout * td + tin)], g.m[2 * (tout * td + tin) + 1]);
+        }
+    }
+}
+
+// B <- G_embedded * B, B row-major 2^nq x 2^nq, G dense on local positions pos[].
+static void left_multiply(std::vector<cd> &B, int nq, const std::vector<int> &pos, const std::vector<cd> &G) {
+    const int dim = 1 << nq, s = (int)pos.size(), gd = 1 << s;
+    uint32_t smask = 0;
+    for (int p : pos) smask |= 1u << p;
+    std::vector<int> offs(gd);
+    for (int r = 0; r < gd; ++r) {
+        int o = 0;
+        for (int j = 0; j < s; ++j) o |= ((r >> j) & 1) << pos[j];
+        offs[r] = o;
+    }
+    std::vector<cd> in(gd), out(gd);
+    for (int base = 0; base < dim; ++base) {
+        if (base & (int)smask) continue;
+        for (int col = 0; col < dim; ++col) {
+            for (int r = 0; r < gd; ++r) in[r] = B[(size_t)(base | offs[r]) * dim + col];
+            for (int r = 0; r < gd; ++r) {
+                cd acc(0, 0);
+                for (int c = 0; c < gd; ++c) acc += G[(size_t)r * gd + c] * in[c];
+                out[r] = acc;
+            }
+            for (int r = 0; r < gd; ++r) B[(size_t)(base | offs[r]) * dim + col] = out[r];
+        }
+    }
+}
+
+// ---------------------------------------------------------------- fuser ---
+std::vector<Block> greedy_partition(const std::vector<Elem> &elems, int n, int kmax) {
+    std::vector<Block> blocks;
+    std::vector<int> remaining(elems.size());
+    for (size_t i = 0; i < elems.size(); ++i) remaining[i] = (int)i;
+    const uint64_t all = n >= 64 ? ~0ull : ((1ull << n) - 1);
+    std::vector<char> taken(elems.size(), 0);
+    while (!remaining.empty()) {
+        Block b;
+        const Elem &first = elems[remaining[0]];
+        const bool first_wide = !first.fusable || __builtin_popcountll(first.mask) > kmax;
+        if (first_wide) {
+            b.members.push_back(remaining[0]);
+            b.mask = first.mask;
+            b.single = true;
+            taken[remaining[0]] = 1;
+        } else {
+            uint64_t Q = 0, blocked_any = 0, blocked_diag = 0;
+            for (int idx : remaining) {
+                const Elem &e = elems[idx];
+                const uint64_t S = e.mask;
+                bool can = e.fusable && __builtin_popcountll(S) <= kmax;
+                if (can) {
+                    if (S & blocked_any) can = false;
+                    else if (!e.diagonal && (S & blocked_diag)) can = false;
+                    else if (__builtin_popcountll(Q | S) > kmax) can = false;
+                }
+                if (can) {
+                    Q |= S;
+                    b.members.push_back(idx);
+                    taken[idx] = 1;
+                } else {
+                    if (e.diagonal && e.fusable) blocked_diag |= S;
+                    else blocked_any |= S;
+                    if ((blocked_any & all) == all) break;
+                }
+            }
+            b.mask = Q;
+            b.single = b.members.size() == 1;
+        }
+        std::vector<int> rest;
+        rest.reserve(remaining.size());
+        for (int idx : remaining)
+            if (!taken[idx]) rest.push_back(idx);
+        remaining.swap(rest);
+        blocks.push_back(std::move(b));
+    }
+    return blocks;
+}
+
+// Dense (or diagonal) matrix of a block on its sorted qubits.
+void compose_block(const std::vector<Elem> &elems, const Block &b, std::vector<int> &qubits, std::vector<cd> &B) {
+    qubits.clear();
+    for (int q = 0; q < 64; ++q)
+        if ((b.mask >> q) & 1ull) qubits.push_back(q);
+    const int nq = (int)qubits.size();
+    const int dim = 1 << nq;
+    B.assign((size_t)dim * dim, cd(0, 0));
+    for (int i = 0; i < dim; ++i) B[(size_t)i * dim + i] = cd(1, 0);
+    std::vector<int> sup, pos;
+    std::vector<cd> D;
+    for (int idx : b.members) {
+        dense_of(elems[idx], sup, D);
+        pos.clear();
+        for (int q : sup) pos.push_back((int)(std::find(qubits.begin(), qubits.end(), q) - qubits.begin()));
+        left_multiply(B, nq, pos, D);
+    }
+}
+
+// ------------------------------------------------------------------ plan ---
+Status build_plan(qi_plan *p, std::vector<Elem> &elems) {
+    const int n = p->n;
+    const int fusion = p->opts.fusion;
+    int kmax = p->opts.max_block_qubits > 0 ? p->opts.max_block_qubits : 6;
+    kmax = std::min(kmax, std::min(6, n));
+    if (p->prec == QI_F64) kmax = std::min(kmax, 5);
+    p->ops.clear();
+    p->mats.clear();
+    std::fill(std::begin(p->stats.n_blocks_by_k), std::end(p->stats.n_blocks_by_k), 0);
+    p->stats.n_gates = (int64_t)elems.size();
+    // Pauli exponentials narrow enough become dense elements when fusing.
+    for (Elem &e : elems) {
+        if (e.pauli && !e.gm.normalise_after && fusion != QI_FUSION_NONE && __builtin_popcountll(e.mask) <= kmax)
+            e.fusable = true;
+    }
+    auto lower_single = [&](const Elem &e) {
+        Op op = lower_gate(n, e.gm);
+        if (op.kind == OP_PAULI_EXP) {
+            const double ar = op.alpha_re, ai = op.alpha_im;
+            op.cre = std::cosh(ar) * std::cos(ai);
+            op.cim = std::sinh(ar) * std::sin(ai);
+            op.sre = std::sinh(ar) * std::cos(ai);
+            op.sim = std::cosh(ar) * std::sin(ai);
+        }
+        if (op.kind != OP_NOP) {
+            p->ops.push_back(op);
+            p->stats.n_blocks_by_k[0]++;
+        }
+    };
+    if (fusion == QI_FUSION_NONE) {
+        for (const Elem &e : elems) lower_single(e);
+    } else {
+        std::vector<Block> blocks = p->partition_override.empty() ? choose_partition(p, elems, kmax)
+                                                                  : p->partition_override;
+        // compose block matrices in parallel (independent)
+        std::vector<std::vector<int>> qb(blocks.size());
+        std::vector<std::vector<cd>> mb(blocks.size());
+        const unsigned nth = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+        std::vector<std::thread> th;
+        for (unsigned w = 0; w < nth; ++w) {
+            th.emplace_back([&, w] {
+                for (size_t bi = w; bi < blocks.size(); bi += nth)
+                    if (!blocks[bi].single) compose_block(elems, blocks[bi], qb[bi], mb[bi]);
+            });
+        }
+        for (auto &t : th) t.join();
+        for (size_t bi = 0; bi < blocks.size(); ++bi) {
+            const Block &b = blocks[bi];
+            if (b.single) { lower_single(elems[b.members[0]]); continue; }
+            bool diag = true;
+            for (int idx : b.members) diag = diag && elems[idx].diagonal;
+            const int k = (int)qb[bi].size();
+            Op op;
+            op.k = k;
+            for (int j = 0; j < k; ++j) op.targets[j] = qb[bi][j];
+            op.mat_offset = (int64_t)p->mats.size();
+            const int dim = 1 << k;
+            if (diag) {
+                op.kind = OP_DIAGK;
+                for (int r = 0; r < dim; ++r) p->mats.push_back(mb[bi][(size_t)r * dim + r]);
+            } else {
+                op.kind = OP_FUSED;
+                op.mode = p->opts.use_tensor_cores;
+                for (size_t i = 0; i < (size_t)dim * dim; ++i) p->mats.push_back(mb[bi][i]);
+            }
+            p->ops.push_back(op);
+            p->stats.n_blocks_by_k[k]++;
+        }
+    }
+    p->stats.n_kernels = (int64_t)p->ops.size();
+    return ok_status();
+}
+
+Status upload_plan(qi_plan *p) {
+    if (p->d_mats) { cudaFree(p->d_mats); p->d_mats = nullptr; }
+    if (p->mats.empty()) return ok_status();
+    const size_t cnt = p->mats.size();
+    if (p->prec == QI_F32) {
+        std::vector<float2> h(cnt);
+        for (size_t i = 0; i < cnt; ++i) h[i] = make_float2((float)p->mats[i].real(), (float)p->mats[i].imag());
+        QI_CUDA(cudaMalloc(&p->d_mats, cnt * sizeof(float2)));
+        QI_CUDA(cudaMemcpy(p->d_mats, h.data(), cnt * sizeof(float2), cudaMemcpyHostToDevice));
+    } else {
+        std::vector<double2> h(cnt);
+        for (size_t i = 0; i < cnt; ++i) h[i] = make_double2(p->mats[i].real(), p->mats[i].imag());
+        QI_CUDA(cudaMalloc(&p->d_mats, cnt * sizeof(double2)));
+        QI_CUDA(cudaMemcpy(p->d_mats, h.data(), cnt * sizeof(double2), cudaMemcpyHostToDevice));
+    }
+    return ok_status();
+}
+
+Status plan_elems_from_gates(int n, const qi_gate *gates, int64_t ng, const double *theta, int64_t ntheta,
+                             std::vector<Elem> &elems) {
+    elems.clear();
+    elems.reserve((size_t)ng);
+    for (int64_t k = 0; k < ng; ++k) {
+        qi_gate g = gates[k];
+        for (int j = 0; j < 3; ++j) {
+            if (g.param_ids[j] >= 0) {
+                if (!theta || g.param_ids[j] >= ntheta)
+                    return err(QI_ERR_MISMATCHED_NUMBER_OF_PARAMETERS, g.param_ids[j] + 1, ntheta);
+                g.params[j] = theta[g.param_ids[j]];
+            }
+        }
+        GateMatrix gm;
+        Status st = gate_to_matrix(n, g, &gm);
+        if (!st.ok()) {
+            st.msg = "gate " + std::to_string(k) + (st.msg.empty() ? "" : ": " + st.msg);
+            return st;
+        }
+        elems.push_back(make_elem_from_gate(gm, (int)k));
+    }
+    return ok_status();
+}
+
+Status plan_execute(qi_plan *p, qi_state *s) {
+    if (s->n != p->n) return err(QI_ERR_INVALID_NUMBER_OF_QUBITS, s->n);   // circuit.rs:161-163
+    if (s->prec != p->prec) return err(QI_ERR_UNSUPPORTED, -1, -1, "plan precision differs from state");
+    if (!p->d_mats && !p->mats.empty()) {   // matrices go to the device on first use
+        Status up = upload_plan(p);
+        if (!up.ok()) return up;
+    }
+    bool has_norm = false;
+    for (const Op &op : p->ops) {
+        Status st = launch_op(s, op, p->d_mats);
+        if (!st.ok()) return st;
+        has_norm = has_norm || op.kind == OP_PAULI_NORM;
+    }
+    if (has_norm) {
+        int flag = 0;
+        Status st = state_read_flag(s, &flag);
+        if (!st.ok()) return st;
+        if (flag) return err(QI_ERR_ZERO_NORM);
+    }
+    return ok_status();
+}
+
+Elem pauli_exp_elem(const qi_pauli_term &t, double far, double fai, int src) {
+    GateMatrix gm;
+    gm.kind = QI_GATE_PAULI_EVOLUTION;
+    gm.pauli = true;
+    gm.xmask = t.xmask;
+    gm.zmask = t.zmask;
+    gm.alpha_re = t.coeff_re * far - t.coeff_im * fai;
+    gm.alpha_im = t.coeff_re * fai + t.coeff_im * far;
+    return make_elem_from_gate(gm, src);
+}
+
+Status sumop_expectation(qi_state *s, const qi_pauli_term *terms, int64_t nt, double out[2]);
+
+}  // namespace qi
+
+using namespace qi;
+
+extern "C" {
+
+qi_status qi_plan_create(int32_t num_qubits, int32_t precision, const qi_gate *gates, int64_t n_gates,
+                         const double *theta, int64_t n_theta, const qi_exec_options *opts, qi_plan **out) {
+    if (!out || (!gates && n_gates > 0)) return publish(err(QI_ERR_NULL_ARGUMENT));
+    *out = nullptr;
+    if (num_qubits <= 0 || num_qubits > 40) return publish(err(QI_ERR_INVALID_NUMBER_OF_QUBITS, num_qubits));
+    if (precision != QI_F32 && precision != QI_F64) return publish(err(QI_ERR_INVALID_INPUT_VALUE, precision));
+    qi_plan *p = new qi_plan();
+    p->n = num_qubits;
+    p->prec = precision;
+    if (opts) p->opts = *opts;
+    std::vector<Elem> elems;
+    Status st = plan_elems_from_gates(num_qubits, gates, n_gates, theta, n_theta, elems);
+    if (st.ok()) st = build_plan(p, elems);
+    if (!st.ok()) { delete p; return publish(st); }
+    *out = p;
+    return publish(ok_status());
+}
+
+qi_status qi_plan_execute(qi_plan *p, qi_state *s) {
+    if (!p || !s) return publish(err(QI_ERR_NULL_ARGUMENT));
+    std::lock_guard<std::recursive_mutex> lk(s->mu);
+    cudaError_t e = cudaSetDevice(s->device);
+    if (e != cudaSuccess) return publish(cuda_status(e, "cudaSetDevice"));
+    return publish(plan_execute(p, s));
+}
+
+qi_status qi_plan_stats_get(const qi_plan *p, qi_plan_stats *out) {
+    if (!p || !out) return publish(err(QI_ERR_NULL_ARGUMENT));
+    *out = p->stats;
+    return publish(ok_status());
+}
+
+qi_status qi_plan_profile(qi_plan *p, qi_state *s, float *ms_out) {
+    if (!p || !s || !ms_out) return publish(err(QI_ERR_NULL_ARGUMENT));
+    std::lock_guard<std::recursive_mutex> lk(s->mu);
+    cudaError_t e = cudaSetDevice(s->device);
+    if (e != cudaSuccess) return publish(cuda_status(e, "cudaSetDevice"));
+    if (s->n != p->n || s->prec != p->prec) return publish(err(QI_ERR_INVALID_NUMBER_OF_QUBITS, s->n));
+    if (!p->d_mats && !p->mats.empty()) {
+        Status up = upload_plan(p);
+        if (!up.ok()) return publish(up);
+    }
+    const size_t nops = p->ops.size();
+    std::vector<cudaEvent_t> ev(nops + 1);
+    for (auto &x : ev) {
+        e = cudaEventCreate(&x);
+        if (e != cudaSuccess) return publish(cuda_status(e, "cudaEventCreate"));
+    }
+    Status st = ok_status();
+    cudaEventRecord(ev[0], s->stream);
+    for (size_t i = 0; i < nops && st.ok(); ++i) {
+        st = launch_op(s, p->ops[i], p->d_mats);
+        cudaEventRecord(ev[i + 1], s->stream);
+    }
+    e = cudaStreamSynchronize(s->stream);
+    if (st.ok() && e != cudaSuccess) st = cuda_status(e, "profile");
+    for (size_t i = 0; i < nops && st.ok(); ++i) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, ev[i], ev[i + 1]);
+        ms_out[i] = ms;
+    }
+    for (auto &x : ev) cudaEventDestroy(x);
+    return publish(st);
+}
+
+qi_status qi_plan_num_ops(const qi_plan *p, int64_t *out) {
+    if (!p || !out) return publish(err(QI_ERR_NULL_ARGUMENT));
+    *out = (int64_t)p->ops.size();
+    return publish(ok_status());
+}
+
+qi_status qi_plan_op_get(const qi_plan *p, int64_t i, qi_plan_op_info *info, double *matrix_out, int64_t capacity) {
+    if (!p || !info) return publish(err(QI_ERR_NULL_ARGUMENT));
+    if (i < 0 || i >= (int64_t)p->ops.size()) return publish(err(QI_ERR_INVALID_INPUT_VALUE, i));
+    const Op &op = p->ops[(size_t)i];
+    std::memset(info, 0, sizeof(*info));
+    info->kind = op.kind;
+    info->k = op.k;
+    for (int j = 0; j < 6; ++j) info->targets[j] = op.targets[j];
+    info->control_mask = op.cmask;
+    info->xmask = op.xmask;
+    info->zmask = op.zmask;
+    std::vector<double> m;
+    switch (op.kind) {
+    case OP_MAT1: m.assign(op.m, op.m + 8); break;
+    case OP_MAT2: m.assign(op.m, op.m + 32); break;
+    case OP_FUSED:
+    case OP_DIAGK: {
+        const size_t cnt = op.kind == OP_FUSED ? ((size_t)1 << (2 * op.k)) : ((size_t)1 << op.k);
+        for (size_t j = 0; j < cnt; ++j) {
+            m.push_back(p->mats[(size_t)op.mat_offset + j].real());
+            m.push_back(p->mats[(size_t)op.mat_offset + j].imag());
+        }
+        break;
+    }
+    case OP_PAULI_EXP: m = {op.cre, op.cim, op.sre, op.sim}; break;
+    default: break;
+    }
+    info->n_matrix = (int64_t)(m.size() / 2);
+    if (matrix_out) {
+        if (capacity < info->n_matrix) return publish(err(QI_ERR_INVALID_INPUT_VALUE, capacity, info->n_matrix));
+        std::copy(m.begin(), m.end(), matrix_out);
+    }
+    return publish(ok_status());
+}
+
+qi_status qi_plan_destroy(qi_plan *p) {
+    if (!p) return QI_OK;
+    if (p->d_mats) cudaFree(p->d_mats);
+    delete p;
+    return QI_OK;
+}
+
+qi_status qi_circuit_execute(qi_state *s, const qi_gate *gates, int64_t n_gates, const double *theta, int64_t n_theta,
+                             const qi_exec_options *opts) {
+    if (!s) return publish(err(QI_ERR_NULL_ARGUMENT));
+    qi_plan *p = nullptr;
+    qi_status st = qi_plan_create(s->n, s->prec, gates, n_gates, theta, n_theta, opts, &p);
+    if (st != QI_OK) return st;
+    st = qi_plan_execute(p, s);
+    if (st == QI_OK) {
+        std::lock_guard<std::recursive_mutex> lk(s->mu);
+        cudaError_t e = cudaStreamSynchronize(s->stream);
+        if (e != cudaSuccess) st = publish(cuda_status(e, "execute"));
+    }
+    qi_plan_destroy(p);
+    return st;
+}
+
+qi_status qi_trotter_evolve(qi_state *s, const qi_pauli_term *terms, int64_t n_terms, double dt, int64_t num_steps,
+                            int32_t order, const qi_pauli_term *observable, int64_t n_obs, int64_t observe_every,
+                            double *energies_out) {
+    if (!s || (!terms && n_terms > 0)) return publish(err(QI_ERR_NULL_ARGUMENT));
+    std::lock_guard<std::recursive_mutex> lk(s->mu);
+    cudaError_t e = cudaSetDevice(s->device);
+    if (e != cudaSuccess) return publish(cuda_status(e, "cudaSetDevice"));
+    if (n_terms == 0) return publish(err(QI_ERR_INVALID_NUMBER_OF_QUBITS, 0));   // time_evolution.rs:51-53
+    if (order != 1 && order != 2) return publish(err(QI_ERR_INVALID_INPUT_VALUE, order));
+    for (int64_t k = 0; k < n_terms; ++k) {
+        Status st = validate_pauli(s->n, terms[k]);
+        if (!st.ok()) return publish(st);
+    }
+    if (observable && observe_every > 0 && !energies_out) return publish(err(QI_ERR_NULL_ARGUMENT));
+    // One step as an ordered list of exponentials (time_evolution.rs:45-115).
+    std::vector<Elem> elems;
+    if (order == 1) {
+        for (int64_t k = 0; k < n_terms; ++k) elems.push_back(pauli_exp_elem(terms[k], 0.0, -dt, (int)k));
+    } else {
+        for (int64_t k = 0; k < n_terms; ++k) elems.push_back(pauli_exp_elem(terms[k], 0.0, -dt / 2.0, (int)k));
+        for (int64_t k = n_terms - 1; k >= 0; --k) elems.push_back(pauli_exp_elem(terms[k], 0.0, -dt / 2.0, (int)k));
+    }
+    qi_plan plan;
+    plan.n = s->n;
+    plan.prec = s->prec;
+    plan.opts.fusion = QI_FUSION_NONE;
+    if (const char *f = std::getenv("QI_TROTTER_FUSION")) plan.opts.fusion = std::atoi(f);
+    plan.opts.max_block_qubits = 0;
+    Status st = build_plan(&plan, elems);
+    if (st.ok()) st = upload_plan(&plan);
+    if (!st.ok()) return publish(st);
+    int64_t obs_k = 0;
+    for (int64_t step = 0; step < num_steps; ++step) {
+        st = plan_execute(&plan, s);
+        if (!st.ok()) break;
+        if (observable && observe_every > 0 && ((step + 1) % observe_every) == 0) {
+            double ev[2];
+            st = sumop_expectation(s, observable, n_obs, ev);
+            if (!st.ok()) break;
+            energies_out[2 * obs_k] = ev[0];
+            energies_out[2 * obs_k + 1] = ev[1];
+            ++obs_k;
+        }
+    }
+    if (plan.d_mats) cudaFree(plan.d_mats);
+    plan.d_mats = nullptr;
+    if (!st.ok()) return publish(st);
+    e = cudaStreamSynchronize(s->stream);
+    if (e != cudaSuccess) return publish(cuda_status(e, "trotter"));
+    return publish(ok_status());
+}
+
+}  // extern "C"

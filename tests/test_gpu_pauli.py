@@ -1,0 +1,102 @@
+"""Pauli kernels, SumOp and Trotter evolution on the GPU vs the oracle."""
+import numpy as np
+import pytest
+
+from quant_iron_gb300 import workloads
+
+pytestmark = pytest.mark.gpu
+
+
+def rand_state(n, seed):
+    rng = np.random.default_rng(seed)
+    v = rng.normal(size=1 << n) + 1j * rng.normal(size=1 << n)
+    return v / np.linalg.norm(v)
+
+
+def rand_terms(n, count, seed, max_weight=3):
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(count):
+        w = int(rng.integers(1, max_weight + 1))
+        qs = rng.choice(n, w, replace=False)
+        ops = [(int(q), "XYZ"[int(rng.integers(0, 3))]) for q in qs]
+        out.append(workloads.term(complex(rng.uniform(-1, 1), rng.uniform(-1, 1) * (rng.random() < 0.3)), ops))
+    return workloads.terms_array(out)
+
+
+@pytest.mark.parametrize("prec", [0, 1], ids=["f64", "f32"])
+def test_pauli_apply_and_exp(qi, orc, prec):
+    tol = 1e-12 if prec == 0 else 2e-6
+    for n in (1, 3, 8, 13):
+        init = rand_state(n, n)
+        for t in rand_terms(n, 12, n, max_weight=min(n, 4)):
+            with qi.DeviceState(n, prec) as st, qi.DeviceState(n, prec) as out:
+                st.upload(init)
+                qi.pauli_apply(out, st, t)
+                assert np.max(np.abs(out.download() - orc.pauli_apply(init, n, t))) < tol
+                qi.pauli_apply_exp_factor(st, t, complex(0.1, -0.37))
+                want = orc.pauli_apply_exp_factor(init, n, t, complex(0.1, -0.37))
+                assert np.max(np.abs(st.download() - want)) < tol * 4
+
+
+@pytest.mark.parametrize("prec", [0, 1], ids=["f64", "f32"])
+def test_sumop_apply_and_expectation(qi, orc, prec):
+    for n in (2, 6, 12):
+        init = rand_state(n, 7 + n)
+        terms = rand_terms(n, 25, n)
+        with qi.DeviceState(n, prec) as st, qi.DeviceState(n, prec) as out:
+            st.upload(init)
+            qi.sumop_apply(out, st, terms)
+            want = orc.sumop_apply(init, n, terms)
+            tol = 1e-11 if prec == 0 else 2e-5
+            assert np.max(np.abs(out.download() - want)) < tol
+            e = qi.sumop_expectation(st, terms)
+            e_want = orc.sumop_expectation(init, n, terms)
+            assert abs(e - e_want) < (1e-11 if prec == 0 else 2e-5)
+
+
+def test_heisenberg_expectation_20q(qi, orc):
+    n = 20
+    init = rand_state(n, 1)
+    terms = workloads.heisenberg_open_chain(n, seed=0)
+    e_want = orc.sumop_expectation(init, n, terms)
+    with qi.DeviceState(n, 0) as st:
+        st.upload(init)
+        assert abs(qi.sumop_expectation(st, terms) - e_want) < 1e-11
+
+
+@pytest.mark.parametrize("order", [1, 2])
+@pytest.mark.parametrize("prec", [0, 1], ids=["f64", "f32"])
+def test_trotter_vs_oracle(qi, orc, prec, order):
+    n = 9
+    terms = workloads.lattice_xyz(3, 3, seed=2)
+    init = workloads.basis_state(n, 0b101100101)
+    want = orc.trotter(init, n, terms, 0.05, 6, order)
+    with qi.DeviceState(n, prec) as st:
+        st.upload(init)
+        energies = qi.trotter_evolve(st, terms, 0.05, 6, order=order, observable=terms, observe_every=3)
+        got = st.download()
+    assert np.max(np.abs(got - want)) < (1e-11 if prec == 0 else 1e-5)
+    assert len(energies) == 2
+    assert abs(energies[-1] - orc.sumop_expectation(want, n, terms)) < (1e-10 if prec == 0 else 1e-4)
+
+
+def test_trotter_errors(qi):
+    with qi.DeviceState(3, 0) as st:
+        st.set_zero()
+        with pytest.raises(qi.QuantIronError) as ei:
+            qi.trotter_evolve(st, workloads.terms_array([]), 0.1, 1)
+        assert ei.value.variant == "InvalidNumberOfQubits" and ei.value.a == 0
+        with pytest.raises(qi.QuantIronError) as ei:
+            qi.trotter_evolve(st, workloads.terms_array([workloads.term(1.0, [(5, "X")])]), 0.1, 1)
+        assert ei.value.variant == "InvalidQubitIndex" and (ei.value.a, ei.value.b) == (5, 3)
+
+
+def test_pauli_normalised_gate(qi, orc):
+    n = 5
+    init = rand_state(n, 4)
+    t = rand_terms(n, 1, 9)[0]
+    with qi.DeviceState(n, 0) as st:
+        st.upload(init)
+        qi.pauli_apply_normalised(st, t)
+        assert np.max(np.abs(st.download() - orc.pauli_apply_normalised(init, n, t))) < 1e-12

@@ -1,0 +1,131 @@
+"""The fusion pass, checked on the CPU: a plan's device operations, replayed in
+numpy, reproduce the oracle's gate-by-gate result (no GPU needed)."""
+import numpy as np
+import pytest
+
+from quant_iron_gb300 import workloads
+
+
+def _apply_local(state, n, targets, mat, cmask=0):
+    """Apply a dense matrix on sorted `targets` (local bit j <-> targets[j]) with controls."""
+    k = len(targets)
+    psi = state.reshape([2] * n)   # axis a <-> qubit n-1-a
+    axes = [n - 1 - t for t in targets[::-1]]   # most significant local bit first
+    rest = [a for a in range(n) if a not in axes]
+    perm = axes + rest
+    t = np.transpose(psi, perm).reshape(1 << k, -1)
+    out = (mat.reshape(1 << k, 1 << k) @ t)
+    # controls: keep columns where control bits are not all set
+    if cmask:
+        cols = np.arange(1 << (n - k))
+        # column index bits <-> `rest` axes, most significant first
+        idx_full = np.zeros_like(cols)
+        for pos, a in enumerate(rest):
+            q = n - 1 - a
+            bit = (cols >> (len(rest) - 1 - pos)) & 1
+            idx_full |= bit << q
+        on = (idx_full & cmask) == cmask
+        out[:, ~on] = t[:, ~on]
+    res = out.reshape([2] * n)
+    inv = np.argsort(perm)
+    return np.transpose(res, inv).reshape(-1)
+
+
+def replay(ops, n, init):
+    s = init.astype(np.complex128).copy()
+    for op in ops:
+        kind = op["kind"]
+        if kind == 1:
+            s = _apply_local(s, n, op["targets"][:1], op["matrix"], op["control_mask"])
+        elif kind == 2:
+            sw = np.zeros(16, dtype=complex)
+            sw[0], sw[1 * 4 + 2], sw[2 * 4 + 1], sw[15] = 1, 1, 1, 1
+            s = _apply_local(s, n, sorted(op["targets"][:2]), sw, op["control_mask"])
+        elif kind == 3:
+            s = _apply_local(s, n, op["targets"][:2], op["matrix"], op["control_mask"])
+        elif kind == 4:
+            s = _apply_local(s, n, op["targets"], op["matrix"], 0)
+        elif kind == 7:
+            s = _apply_local(s, n, op["targets"], np.diag(op["matrix"]).reshape(-1), 0)
+        elif kind == 5:
+            x, z = op["xmask"], op["zmask"]
+            ch, sh = op["matrix"][0], op["matrix"][1]
+            idx = np.arange(1 << n)
+            ny = bin(x & z).count("1")
+            ph = (-1j) ** ny * np.where(np.array([bin(i & z).count("1") % 2 for i in idx]) == 1, -1, 1)
+            s = ch * s + sh * ph * s[idx ^ x]
+        else:
+            raise AssertionError("unexpected op kind %d" % kind)
+    return s
+
+
+@pytest.mark.parametrize("kmax", [2, 3, 4, 5, 6])
+@pytest.mark.parametrize("seed", [0, 1, 2])
+def test_greedy_fusion_replay_matches_oracle(qi, orc, kmax, seed):
+    n = 8
+    gates = workloads.random_circuit(n, layers=5, seed=seed)
+    init = workloads.plus_state(n)
+    want = orc.execute(init, n, gates)
+    plan = qi.Plan(n, qi.F64, gates, fusion=qi.FUSION_GREEDY, max_block_qubits=kmax)
+    ops = plan.ops()
+    assert all(op["k"] <= kmax for op in ops)
+    got = replay(ops, n, init)
+    assert np.max(np.abs(got - want)) < 1e-12
+    st = plan.stats()
+    assert st["n_kernels"] == len(ops) < len(gates)
+
+
+def test_per_gate_plan_replay_matches_oracle(qi, orc):
+    n = 7
+    gates = workloads.random_circuit(n, layers=4, seed=11)
+    init = workloads.plus_state(n)
+    plan = qi.Plan(n, qi.F64, gates, fusion=qi.FUSION_NONE)
+    assert plan.stats()["n_kernels"] == len(gates)
+    assert np.max(np.abs(replay(plan.ops(), n, init) - orc.execute(init, n, gates))) < 1e-12
+
+
+def test_fusion_with_controls_matchgate_toffoli(qi, orc):
+    from quant_iron_gb300.workloads import GateList
+    n = 6
+    gl = GateList()
+    rng = np.random.default_rng(5)
+    for _ in range(30):
+        q = int(rng.integers(0, n - 1))
+        gl.add("MATCHGATE", [q], [int((q + 2) % n)] if q + 2 < n else [], [rng.uniform(0, 6), rng.uniform(0, 6),
+                                                                           rng.uniform(0, 6)])
+        gl.add("TOFFOLI", [int(rng.integers(0, 2))], [2, 3])
+        gl.add("RX", [int(rng.integers(0, n))], [], [rng.uniform(0, 6)])
+        gl.add("SWAP", [1, 4], [0])
+        # control on q2 of the matchgate (the (01,10) rotation is then disabled)
+        gl.add("MATCHGATE", [2], [3], [1.1, 0.3, 0.7])
+    gates = gl.array()
+    init = orc.execute(workloads.plus_state(n), n, workloads.random_circuit(n, 2, seed=1, with_qft=False))
+    want = orc.execute(init, n, gates)
+    for kmax in (3, 4, 6):
+        plan = qi.Plan(n, qi.F64, gates, fusion=qi.FUSION_GREEDY, max_block_qubits=kmax)
+        assert np.max(np.abs(replay(plan.ops(), n, init) - want)) < 1e-12
+
+
+def test_pauli_evolution_gates_fuse(qi, orc):
+    from quant_iron_gb300.workloads import GateList
+    n = 6
+    gl = GateList()
+    rng = np.random.default_rng(2)
+    for _ in range(20):
+        a, b = rng.choice(n, 2, replace=False)
+        x = (1 << int(a)) if rng.random() < 0.5 else 0
+        z = (1 << int(b)) | (1 << int(a) if rng.random() < 0.5 else 0)
+        gl.add("PAULI_EVOLUTION", [], [], [rng.uniform(-1, 1), 0.0, 0.07], xmask=x, zmask=z)
+        gl.add("H", [int(rng.integers(0, n))])
+    gates = gl.array()
+    init = workloads.plus_state(n)
+    want = orc.execute(init, n, gates)
+    plan = qi.Plan(n, qi.F64, gates, fusion=qi.FUSION_GREEDY, max_block_qubits=4)
+    assert np.max(np.abs(replay(plan.ops(), n, init) - want)) < 1e-12
+
+
+def test_qft_diagonal_runs_fuse(qi):
+    n = 20
+    gates = workloads.qft(workloads.GateList(), list(range(n))).array()
+    st = qi.Plan(n, qi.F32, gates, fusion=qi.FUSION_GREEDY, max_block_qubits=6).stats()
+    assert st["n_kernels"] < len(gates) / 3

@@ -254,10 +254,13 @@ def main():
     value = world * LAYERS * args.steps / (ms / 1e3)
 
     # per-op device times of one execution (events on the launching stream)
+    st.set_plus()
     ops, op_ms = qi.plan_profile(plan, st)
     by_kernel = {}
     for op, t in zip(ops, op_ms):
         name = qi.KERNEL_OF_OP_KIND.get(op["kind"], str(op["kind"]))
+        if op["kind"] == 4:
+            name = "k_fused_tc" if op.get("tensor_cores") else "k_fused_simt"
         d = by_kernel.setdefault(name, {"launches": 0, "ms": 0.0})
         d["launches"] += 1
         d["ms"] += t

@@ -195,6 +195,12 @@ typedef struct qi_gate {
  * (operator.rs:214-273) plus the per-gate checks (CNOT control count,
  * Toffoli controls, Matchgate last qubit). */
 qi_status qi_apply_gate(qi_state *s, const qi_gate *g);
+/* Apply a dense 2^k x 2^k complex matrix (row-major interleaved f64 pairs,
+ * local bit j <-> targets[j]) to k distinct qubits, k <= 6; one HBM pass.
+ * Generalises Unitary2::apply (operator.rs:2206-2266) to k qubits; no
+ * unitarity check.  use_tensor_cores as in qi_exec_options. */
+qi_status qi_apply_matrix(qi_state *s, const int32_t *targets, int32_t k, const double *matrix,
+                          int32_t use_tensor_cores);
 /* `Unitary2::new` unitarity check (operator.rs:2092-2125), tol 2*eps. */
 qi_status qi_unitary2_check(const double m[8]);
 
@@ -243,8 +249,11 @@ qi_status qi_trotter_evolve(qi_state *s, const qi_pauli_term *terms, int64_t n_t
 typedef struct qi_exec_options {
     int32_t fusion;            /* QI_FUSION_* */
     int32_t max_block_qubits;  /* k <= 6; 0 = default (6) */
-    int32_t use_tensor_cores;  /* 1 = 3xTF32 tcgen05 kernel for FP32 blocks of k >= 5, 0 = CUDA cores only */
-    int32_t reserved;
+    int32_t use_tensor_cores;  /* 0 or 1: 3xTF32 tcgen05 kernel for FP32 blocks of k >= 5 (default); 2: CUDA cores only */
+    int32_t renorm_every;      /* FP64 renormalisation on the device: 0 = once at the end when tensor-core
+                                  blocks ran (their FP32 accumulation rounds toward zero, so the norm drifts
+                                  down by ~1e-6 per block); N > 0 = also after every N tensor-core blocks;
+                                  -1 = never */
 } qi_exec_options;
 
 typedef struct qi_plan_stats {
@@ -273,6 +282,8 @@ typedef struct qi_plan_op_info {
                                5 Pauli exponential, 6 Pauli string + normalise, 7 diagonal block */
     int32_t  k;             /* number of targets */
     int32_t  targets[6];    /* sorted ascending for kinds 3, 4, 7 */
+    int32_t  tensor_cores;  /* kind 4: 1 if the block runs on the tcgen05 tensor-core kernel */
+    int32_t  reserved;
     uint64_t control_mask;
     uint64_t xmask, zmask;  /* kinds 5 and 6 */
     int64_t  n_matrix;      /* complex entries of the op's matrix: 4 (kind 1), 16 (kind 3), 4^k (kind 4),

@@ -158,8 +158,8 @@ def tensor_product(out, a, b):
     check(lib.qi_state_tensor_product(out.h, a.h, b.h))
 
 
-def _options(fusion, max_block_qubits=0, use_tensor_cores=0):
-    return _abi.ExecOptions(int(fusion), int(max_block_qubits), int(use_tensor_cores), 0)
+def _options(fusion, max_block_qubits=0, use_tensor_cores=0, renorm_every=0):
+    return _abi.ExecOptions(int(fusion), int(max_block_qubits), int(use_tensor_cores), int(renorm_every))
 
 
 def _theta_arg(theta):
@@ -173,10 +173,10 @@ class Plan:
     """A validated, compiled gate list for one qubit count and precision."""
 
     def __init__(self, num_qubits, precision, gates, theta=None, fusion=FUSION_NONE, max_block_qubits=0,
-                 use_tensor_cores=0):
+                 use_tensor_cores=0, renorm_every=0):
         gates = np.ascontiguousarray(gates, dtype=GATE_DTYPE)
         self.h = ctypes.c_void_p()
-        opts = _options(fusion, max_block_qubits, use_tensor_cores)
+        opts = _options(fusion, max_block_qubits, use_tensor_cores, renorm_every)
         tp, tn, self._keep = _theta_arg(theta)
         check(lib.qi_plan_create(int(num_qubits), int(precision), gates.ctypes.data if gates.size else None,
                                  gates.size, tp, tn, ctypes.byref(opts), ctypes.byref(self.h)))
@@ -204,6 +204,7 @@ class Plan:
                                      info.n_matrix))
             mat = buf[0::2][:info.n_matrix] + 1j * buf[1::2][:info.n_matrix]
             out.append({"kind": info.kind, "k": info.k, "targets": list(info.targets)[:max(info.k, 0)],
+                        "tensor_cores": info.tensor_cores,
                         "control_mask": info.control_mask, "xmask": info.xmask, "zmask": info.zmask,
                         "matrix": mat})
         return out
@@ -220,10 +221,11 @@ class Plan:
             pass
 
 
-def circuit_execute(state, gates, theta=None, fusion=FUSION_NONE, max_block_qubits=0, use_tensor_cores=0):
+def circuit_execute(state, gates, theta=None, fusion=FUSION_NONE, max_block_qubits=0, use_tensor_cores=0,
+                    renorm_every=0):
     """Circuit::execute (src/circuit.rs:160-172) on a resident state (in place)."""
     gates = np.ascontiguousarray(gates, dtype=GATE_DTYPE)
-    opts = _options(fusion, max_block_qubits, use_tensor_cores)
+    opts = _options(fusion, max_block_qubits, use_tensor_cores, renorm_every)
     tp, tn, _keep = _theta_arg(theta)
     check(lib.qi_circuit_execute(state.h, gates.ctypes.data if gates.size else None, gates.size, tp, tn,
                                  ctypes.byref(opts)))
@@ -293,7 +295,7 @@ def trotter_evolve(state, terms, dt, num_steps, order=1, observable=None, observ
 
 
 KERNEL_OF_OP_KIND = {1: "k_mat1", 2: "k_swap", 3: "k_mat2", 4: "k_fused", 5: "k_pauli_exp", 6: "k_pauli_exp+normalise",
-                     7: "k_diagk"}
+                     7: "k_diagk", 8: "k_norm_partial+k_normalise_apply"}
 
 
 def plan_profile(plan, state):
@@ -303,3 +305,11 @@ def plan_profile(plan, state):
     ms = (ctypes.c_float * max(1, len(ops)))()
     check(lib.qi_plan_profile(plan.h, state.h, ms))
     return ops, [float(ms[i]) for i in range(len(ops))]
+
+
+def apply_matrix(state, targets, matrix, use_tensor_cores=0):
+    """Dense 2^k x 2^k matrix on `targets` (local bit j <-> targets[j]), one HBM pass."""
+    t = np.ascontiguousarray(targets, dtype=np.int32)
+    m = np.ascontiguousarray(matrix, dtype=np.complex128).reshape(-1).view(np.float64)
+    check(lib.qi_apply_matrix(state.h, t.ctypes.data, t.size, m.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                              int(use_tensor_cores)))

@@ -71,7 +71,7 @@ class ErrorInfo(ctypes.Structure):
 
 class ExecOptions(ctypes.Structure):
     _fields_ = [("fusion", ctypes.c_int32), ("max_block_qubits", ctypes.c_int32),
-                ("use_tensor_cores", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+                ("use_tensor_cores", ctypes.c_int32), ("renorm_every", ctypes.c_int32)]
 
 
 class PlanStats(ctypes.Structure):
@@ -81,6 +81,7 @@ class PlanStats(ctypes.Structure):
 
 class PlanOpInfo(ctypes.Structure):
     _fields_ = [("kind", ctypes.c_int32), ("k", ctypes.c_int32), ("targets", ctypes.c_int32 * 6),
+                ("tensor_cores", ctypes.c_int32), ("reserved", ctypes.c_int32),
                 ("control_mask", ctypes.c_uint64), ("xmask", ctypes.c_uint64), ("zmask", ctypes.c_uint64),
                 ("n_matrix", ctypes.c_int64)]
 
@@ -174,3 +175,5 @@ def check(status):
 
 lib.qi_plan_profile.restype = _i32
 lib.qi_plan_profile.argtypes = [_vp, _vp, ctypes.POINTER(ctypes.c_float)]
+lib.qi_apply_matrix.restype = _i32
+lib.qi_apply_matrix.argtypes = [_vp, _vp, _i32, _pd, _i32]

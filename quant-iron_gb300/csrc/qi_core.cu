@@ -171,10 +171,12 @@ __global__ void k_normalise_apply(typename Cx<T>::V2 *a, uint64_t dim, const dou
         return;
     }
     if (norm == 1.0) return;
+    const T inv = (T)(1.0 / norm);
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < dim; i += (uint64_t)gridDim.x * blockDim.x) {
         typename Cx<T>::V2 v = a[i];
-        if constexpr (sizeof(T) == 8) a[i] = Cx<T>::make(v.x / norm, v.y / norm);
-        else a[i] = Cx<T>::make((float)((double)v.x / norm), (float)((double)v.y / norm));
+        // multiply by the reciprocal (within 1 ulp of x / norm): FP64 division is
+        // tens of FP64 operations, and FP64 is the GB300's slowest pipe
+        a[i] = Cx<T>::make(v.x * inv, v.y * inv);
     }
 }
 

@@ -5,251 +5,227 @@
 // pass: out[r'][c] = sum_r U[r'][r] in[r][c], where r is the target-bit
 // pattern of an amplitude index and c the pattern of the other qubits.
 //
-// Tiling: a CTA tile holds all 2^k target patterns for 2^nb "columns", the
-// columns being the nb lowest non-target qubits.  Every qubit below the
-// highest of those is in the tile, so the tile is 2^h contiguous runs of
-// global memory (h = targets above that point): the load and store are
-// coalesced 16-byte accesses.  In shared memory the tile is stored
-// transposed as [2^k rows][2^nb + 1 columns] (one padding element per row):
-// the scatter from address order and the per-column reads of the compute
-// phase are both free of bank conflicts.
-// Compute: thread j owns column j, holds its 2^k amplitudes in registers and
-// forms the matrix-vector product with U read from shared memory (broadcast).
+// Tiles and their shared-memory layout are described in qi_tile.cuh.  This
+// file holds the CUDA-core kernel (any k <= 6, FP32 or FP64) and the
+// diagonal-block kernel; the tensor-core kernel is in qi_fused_tc.cu.
 #include "qi_internal.hpp"
 #include "qi_device.cuh"
+#include "qi_tile.cuh"
 
 #include <algorithm>
 
 namespace qi {
 
-struct FusedParams {
-    uint64_t ntiles;
-    int32_t k, nb, L;        // targets, column bits, width of the contiguous low run
-    int32_t nlow_t;          // targets below L
-    int32_t nhigh;           // targets at or above L
-    int8_t low_t[8];         // target positions below L (ascending)
-    int8_t high_t[8];        // target positions >= L (ascending)
-    int8_t free_pos[64];     // qubits outside the tile (ascending): tile index -> base address
-    int32_t nfree;
-};
+constexpr int kSimtThreads = 256;
 
-template <typename T>
-__device__ __forceinline__ void tile_coords(const FusedParams &p, uint32_t x, uint32_t &r, uint32_t &c, uint64_t &goff) {
-    // x: tile-local index in address order = (xh << L) | xl
-    const uint32_t xl = x & ((1u << p.L) - 1), xh = x >> p.L;
-    // r_lo = pext(xl, low targets); c = xl with low-target bits removed
-    uint32_t rl = 0, cc = xl;
-    for (int j = p.nlow_t - 1; j >= 0; --j) {
-        const int q = p.low_t[j];
-        rl = (rl << 1) | ((xl >> q) & 1u);
-        cc = ((cc >> (q + 1)) << q) | (cc & ((1u << q) - 1));
-    }
-    r = rl | (xh << p.nlow_t);
-    c = cc;
-    uint64_t g = xl;
-    for (int j = 0; j < p.nhigh; ++j) g |= (uint64_t)((xh >> j) & 1u) << p.high_t[j];
-    goff = g;
-}
-
-template <typename T, int K, int B>
-__global__ void __launch_bounds__(1 << B) k_fused_simt(typename Cx<T>::V2 *a, const typename Cx<T>::V2 *mat,
-                                                       FusedParams p) {
+// Fused block on CUDA cores.  Persistent CTAs walk the tiles; tile t + 2*grid
+// is prefetched with cp.async into the buffer tile t just released, so loads
+// overlap the matrix-vector work of the other buffer.  Each column's 2^K
+// amplitudes are read into registers, multiplied by U (read from shared
+// memory as a broadcast) and written back in place; when several threads
+// share a column (few columns per tile) each computes a slice of the rows,
+// after all of them have read the inputs.
+template <typename T, int K>
+__global__ void __launch_bounds__(kSimtThreads) k_fused_simt(typename Cx<T>::V2 *a, const typename Cx<T>::V2 *mat,
+                                                             TileGeom g) {
     using V2 = typename Cx<T>::V2;
     constexpr int R = 1 << K;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     V2 *sm_mat = reinterpret_cast<V2 *>(smem_raw);
-    V2 *tile = sm_mat + R * R;
-    const int ncol = 1 << p.nb;
-    const int ld = ncol + 1;
-    const uint32_t tile_amps = (uint32_t)R << p.nb;
+    TileIterTab *tab = reinterpret_cast<TileIterTab *>(sm_mat + R * R);
+    V2 *S0 = reinterpret_cast<V2 *>(tab + 32);
+    const uint32_t tile_amps = 1u << (K + g.nb);
+    V2 *S1 = S0 + tile_amps;
+    const int tid = threadIdx.x;
+    const int ncol = 1 << g.nb;
 
-    for (int i = threadIdx.x; i < R * R; i += blockDim.x) sm_mat[i] = mat[i];
+    for (int i = tid; i < R * R; i += kSimtThreads) sm_mat[i] = mat[i];
+    const TileWalk w = tile_walk_init(g, tid, kSimtThreads);
+    if (tid < w.iters) tile_iter_fill(g, kSimtThreads, tid, tab);
+    __syncthreads();
 
-    for (uint64_t t = blockIdx.x; t < p.ntiles; t += gridDim.x) {
-        // base address of this tile: deposit t into the non-tile qubits
-        uint64_t base = 0;
-        for (int j = 0; j < p.nfree; ++j) base |= ((t >> j) & 1ull) << p.free_pos[j];
-        __syncthreads();   // previous tile fully stored / matrix loaded
-        // load (qubit 0 is always in the tile, so pairs (x, x+1) are adjacent)
-        if constexpr (sizeof(T) == 4) {
-            const float4 *a4 = reinterpret_cast<const float4 *>(a);
-            for (uint32_t v = threadIdx.x; v < tile_amps / 2; v += blockDim.x) {
-                uint32_t r0, c0, r1, c1;
-                uint64_t g0, g1;
-                tile_coords<T>(p, 2 * v, r0, c0, g0);
-                tile_coords<T>(p, 2 * v + 1, r1, c1, g1);
-                float4 q = __ldcs(a4 + ((base | g0) >> 1));
-                tile[r0 * ld + c0] = make_float2(q.x, q.y);
-                tile[r1 * ld + c1] = make_float2(q.z, q.w);
-            }
-        } else {
-            for (uint32_t x = threadIdx.x; x < tile_amps; x += blockDim.x) {
-                uint32_t r, c;
-                uint64_t g;
-                tile_coords<T>(p, x, r, c, g);
-                tile[r * ld + c] = __ldcs(a + (base | g));
-            }
-        }
+    // column / row-slice assignment
+    const int split = ncol >= kSimtThreads ? 1 : min(R, kSimtThreads / ncol);
+    const int rows_per = R / split;
+    const int col0 = tid % (ncol >= kSimtThreads ? kSimtThreads : ncol);
+    const int part = ncol >= kSimtThreads ? 0 : tid / ncol;
+    const bool computes = part < split;
+
+    uint64_t t = blockIdx.x;
+    if (t < g.ntiles) tile_load_async(g, w, tab, a, tile_base(g, t), S0);
+    cp_async_commit();
+    if (t + gridDim.x < g.ntiles) tile_load_async(g, w, tab, a, tile_base(g, t + gridDim.x), S1);
+    cp_async_commit();
+    for (int it = 0; t < g.ntiles; ++it, t += gridDim.x) {
+        V2 *S = (it & 1) ? S1 : S0;
+        cp_async_wait<1>();
         __syncthreads();
-        // compute: column j
-        for (int j = threadIdx.x; j < ncol; j += blockDim.x) {
-            V2 in[R];
+        if (computes) {
+            for (int j = col0; j < ncol; j += kSimtThreads) {
+                V2 in[R];
 #pragma unroll
-            for (int r = 0; r < R; ++r) in[r] = tile[r * ld + j];
+                for (int r = 0; r < R; ++r) in[r] = S[tile_sidx(g, r, j)];
+                if (split > 1) __syncthreads();   // every slice has read the column
 #pragma unroll 1
-            for (int ro = 0; ro < R; ++ro) {
-                const V2 *mrow = sm_mat + ro * R;
-                T accx = 0, accy = 0;
+                for (int ro = part * rows_per; ro < (part + 1) * rows_per; ++ro) {
+                    const V2 *mrow = sm_mat + ro * R;
+                    T ax = 0, ay = 0;
 #pragma unroll
-                for (int r = 0; r < R; ++r) {
-                    const V2 m = mrow[r];
-                    accx = ::fma(m.x, in[r].x, accx);
-                    accx = ::fma(-m.y, in[r].y, accx);
-                    accy = ::fma(m.x, in[r].y, accy);
-                    accy = ::fma(m.y, in[r].x, accy);
+                    for (int r = 0; r < R; ++r) {
+                        const V2 m = mrow[r];
+                        ax = ::fma(m.x, in[r].x, ax);
+                        ax = ::fma(-m.y, in[r].y, ax);
+                        ay = ::fma(m.x, in[r].y, ay);
+                        ay = ::fma(m.y, in[r].x, ay);
+                    }
+                    S[tile_sidx(g, ro, j)] = Cx<T>::make(ax, ay);
                 }
-                tile[ro * ld + j] = Cx<T>::make(accx, accy);
             }
+        } else if (split > 1) {
+            __syncthreads();   // match the barrier of the computing threads
         }
         __syncthreads();
-        // store
-        if constexpr (sizeof(T) == 4) {
-            float4 *a4 = reinterpret_cast<float4 *>(a);
-            for (uint32_t v = threadIdx.x; v < tile_amps / 2; v += blockDim.x) {
-                uint32_t r0, c0, r1, c1;
-                uint64_t g0, g1;
-                tile_coords<T>(p, 2 * v, r0, c0, g0);
-                tile_coords<T>(p, 2 * v + 1, r1, c1, g1);
-                const float2 u = tile[r0 * ld + c0], w = tile[r1 * ld + c1];
-                __stcs(a4 + ((base | g0) >> 1), make_float4(u.x, u.y, w.x, w.y));
-            }
-        } else {
-            for (uint32_t x = threadIdx.x; x < tile_amps; x += blockDim.x) {
-                uint32_t r, c;
-                uint64_t g;
-                tile_coords<T>(p, x, r, c, g);
-                __stcs(a + (base | g), tile[r * ld + c]);
-            }
-        }
+        tile_store(g, w, tab, a, tile_base(g, t), S);
+        __syncthreads();
+        const uint64_t nt = t + 2ull * gridDim.x;
+        if (nt < g.ntiles) tile_load_async(g, w, tab, a, tile_base(g, nt), S);
+        cp_async_commit();
     }
+    cp_async_wait<0>();
 }
 
-// Diagonal block: a[i] *= phase[pext(i, targets)].
+// Diagonal block: a[i] *= phase[pext(i, targets)].  Each thread handles
+// kDiagUnroll independent 16-byte vectors per iteration (2 FP32 or 1 FP64
+// amplitude each) so that enough bytes are in flight to saturate HBM.
+constexpr int kDiagUnroll = 4;
+
+struct DiagParams {
+    uint64_t nvec;       // number of 16-byte vectors
+    int32_t k;
+    int8_t pos[10];      // target positions, ascending
+};
+
+__device__ __forceinline__ uint32_t pext_pos(uint64_t i, const DiagParams &p) {
+    uint32_t r = 0;
+#pragma unroll
+    for (int b = 0; b < 10; ++b)
+        if (b < p.k) r |= (uint32_t)((i >> p.pos[b]) & 1ull) << b;
+    return r;
+}
+
 template <typename T>
-__global__ void __launch_bounds__(256) k_diagk(typename Cx<T>::V2 *a, uint64_t dim, const typename Cx<T>::V2 *ph,
-                                               int k, uint64_t tmask) {
+__global__ void __launch_bounds__(256) k_diagk(typename Cx<T>::V2 *a, const typename Cx<T>::V2 *ph, DiagParams p) {
     using V2 = typename Cx<T>::V2;
     __shared__ V2 sph[1 << 10];
-    const int R = 1 << k;
+    const int R = 1 << p.k;
     for (int i = threadIdx.x; i < R; i += blockDim.x) sph[i] = ph[i];
     __syncthreads();
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < dim; i += stride) {
-        // pext(i, tmask)
-        uint32_t r = 0;
-        uint64_t m = tmask;
-        int b = 0;
-        while (m) {
-            const int q = __ffsll((long long)m) - 1;
-            r |= (uint32_t)((i >> q) & 1ull) << b;
-            ++b;
-            m &= m - 1;
+    for (uint64_t base = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; base < p.nvec; base += stride * kDiagUnroll) {
+        if constexpr (sizeof(T) == 4) {
+            float4 *a4 = reinterpret_cast<float4 *>(a);
+            float4 v[kDiagUnroll];
+#pragma unroll
+            for (int u = 0; u < kDiagUnroll; ++u) {
+                const uint64_t j = base + u * stride;
+                if (j < p.nvec) v[u] = __ldcs(a4 + j);
+            }
+#pragma unroll
+            for (int u = 0; u < kDiagUnroll; ++u) {
+                const uint64_t j = base + u * stride;
+                if (j < p.nvec) {
+                    const float2 x = Cx<float>::mul(sph[pext_pos(2 * j, p)], make_float2(v[u].x, v[u].y));
+                    const float2 y = Cx<float>::mul(sph[pext_pos(2 * j + 1, p)], make_float2(v[u].z, v[u].w));
+                    __stcs(a4 + j, make_float4(x.x, x.y, y.x, y.y));
+                }
+            }
+        } else {
+            double2 v[kDiagUnroll];
+#pragma unroll
+            for (int u = 0; u < kDiagUnroll; ++u) {
+                const uint64_t j = base + u * stride;
+                if (j < p.nvec) v[u] = __ldcs(reinterpret_cast<const double2 *>(a) + j);
+            }
+#pragma unroll
+            for (int u = 0; u < kDiagUnroll; ++u) {
+                const uint64_t j = base + u * stride;
+                if (j < p.nvec) __stcs(reinterpret_cast<double2 *>(a) + j, Cx<double>::mul(sph[pext_pos(j, p)], v[u]));
+            }
         }
-        V2 v = a[i];
-        a[i] = Cx<T>::mul(sph[r], v);
     }
 }
 
-static int column_bits(int prec, int k) {
-    if (prec == QI_F32) return k <= 5 ? 8 : 7;
-    return k <= 4 ? 8 : (k == 5 ? 7 : 6);
-}
+// Column bits per tile: 2^(K + nb) amplitudes = 32 KB per buffer.
+static int column_bits(int prec, int k) { return (prec == QI_F32 ? 12 : 11) - k; }
 
-template <typename T, int K, int B>
-static Status launch_simt_t(qi_state *s, const FusedParams &p, const void *d_mat) {
+template <typename T, int K>
+static Status launch_simt_t(qi_state *s, const TileGeom &g, const void *d_mat) {
     constexpr int R = 1 << K;
-    const size_t smem = (size_t)R * R * sizeof(typename Cx<T>::V2) +
-                        (size_t)R * ((1 << p.nb) + 1) * sizeof(typename Cx<T>::V2);
-    auto kern = k_fused_simt<T, K, B>;
+    using V2 = typename Cx<T>::V2;
+    const size_t smem = (size_t)R * R * sizeof(V2) + 32 * sizeof(TileIterTab) + 2 * ((size_t)R << g.nb) * sizeof(V2);
+    auto kern = k_fused_simt<T, K>;
     static bool attr_set = false;   // per instantiation
     if (!attr_set) {
         QI_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
         attr_set = true;
     }
-    int dev_sms = 152;
-    uint64_t grid = p.ntiles;
-    const uint64_t cap = (uint64_t)dev_sms * (smem <= 70 * 1024 ? 3 : (smem <= 110 * 1024 ? 2 : 1)) * 4;
+    int per_sm = 0;
+    QI_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kSimtThreads, smem));
+    if (per_sm < 1) per_sm = 1;
+    uint64_t grid = g.ntiles;
+    const uint64_t cap = (uint64_t)152 * per_sm;
     if (grid > cap) grid = cap;
-    kern<<<(unsigned)grid, 1 << B, smem, s->stream>>>((typename Cx<T>::V2 *)s->amps,
-                                                     (const typename Cx<T>::V2 *)d_mat, p);
+    kern<<<(unsigned)grid, kSimtThreads, smem, s->stream>>>((V2 *)s->amps, (const V2 *)d_mat, g);
     count_launch();
     return check_launch("k_fused_simt");
 }
 
-Status launch_fused(qi_state *s, int k, const int32_t *targets, const void *d_mat, int use_tc) {
-    (void)use_tc;
+Status launch_fused_simt(qi_state *s, int k, const int32_t *targets, const void *d_mat) {
     const int n = s->n;
-    if (k < 1 || k > 6 || k > n) return err(QI_ERR_INVALID_INPUT_VALUE, k, n, "fused block width");
-    if (s->prec == QI_F64 && k > 5) return err(QI_ERR_UNSUPPORTED, k, -1, "FP64 fused blocks are limited to k <= 5");
-    FusedParams p;
-    std::memset(&p, 0, sizeof(p));
-    p.k = k;
-    uint64_t tmask = 0;
-    for (int j = 0; j < k; ++j) tmask |= 1ull << targets[j];
-    const int bmax = column_bits(s->prec, k);
-    p.nb = std::min(bmax, n - k);
-    // columns: the nb lowest non-target qubits; L = one past the highest of them
-    int got = 0, q = 0;
-    while (got < p.nb) {
-        if (!((tmask >> q) & 1ull)) ++got;
-        ++q;
-    }
-    // if nb == 0 every qubit is a target: L = number of low targets contiguous from 0
-    if (p.nb == 0) q = 0;
-    // extend L over targets directly above the columns (still contiguous)
-    while (q < n && ((tmask >> q) & 1ull)) ++q;
-    p.L = q;
-    p.nlow_t = 0;
-    p.nhigh = 0;
-    for (int j = 0; j < k; ++j) {
-        if (targets[j] < p.L) p.low_t[p.nlow_t++] = (int8_t)targets[j];
-        else p.high_t[p.nhigh++] = (int8_t)targets[j];
-    }
-    p.nfree = 0;
-    for (int qq = 0; qq < n; ++qq)
-        if (qq >= p.L && !((tmask >> qq) & 1ull)) p.free_pos[p.nfree++] = (int8_t)qq;
-    p.ntiles = 1ull << p.nfree;
-    if (p.nfree != n - k - p.nb) return err(QI_ERR_UNKNOWN, p.nfree, n - k - p.nb, "tile decomposition");
+    const int nb = std::min(column_bits(s->prec, k), n - k);
+    const TileGeom g = make_tile_geom(n, k, targets, nb);
+    if (g.nfree != n - k - nb) return err(QI_ERR_UNKNOWN, g.nfree, n - k - nb, "tile decomposition");
     if (s->prec == QI_F32) {
         switch (k) {
-        case 1: return launch_simt_t<float, 1, 8>(s, p, d_mat);
-        case 2: return launch_simt_t<float, 2, 8>(s, p, d_mat);
-        case 3: return launch_simt_t<float, 3, 8>(s, p, d_mat);
-        case 4: return launch_simt_t<float, 4, 8>(s, p, d_mat);
-        case 5: return launch_simt_t<float, 5, 8>(s, p, d_mat);
-        default: return launch_simt_t<float, 6, 7>(s, p, d_mat);
+        case 1: return launch_simt_t<float, 1>(s, g, d_mat);
+        case 2: return launch_simt_t<float, 2>(s, g, d_mat);
+        case 3: return launch_simt_t<float, 3>(s, g, d_mat);
+        case 4: return launch_simt_t<float, 4>(s, g, d_mat);
+        case 5: return launch_simt_t<float, 5>(s, g, d_mat);
+        default: return launch_simt_t<float, 6>(s, g, d_mat);
         }
     }
     switch (k) {
-    case 1: return launch_simt_t<double, 1, 8>(s, p, d_mat);
-    case 2: return launch_simt_t<double, 2, 8>(s, p, d_mat);
-    case 3: return launch_simt_t<double, 3, 8>(s, p, d_mat);
-    case 4: return launch_simt_t<double, 4, 8>(s, p, d_mat);
-    default: return launch_simt_t<double, 5, 7>(s, p, d_mat);
+    case 1: return launch_simt_t<double, 1>(s, g, d_mat);
+    case 2: return launch_simt_t<double, 2>(s, g, d_mat);
+    case 3: return launch_simt_t<double, 3>(s, g, d_mat);
+    case 4: return launch_simt_t<double, 4>(s, g, d_mat);
+    default: return launch_simt_t<double, 5>(s, g, d_mat);
     }
+}
+
+Status launch_fused(qi_state *s, int k, const int32_t *targets, const void *d_mat, const void *d_tc, int use_tc) {
+    const int n = s->n;
+    if (k < 1 || k > 6 || k > n) return err(QI_ERR_INVALID_INPUT_VALUE, k, n, "fused block width");
+    if (s->prec == QI_F64 && k > 5) return err(QI_ERR_UNSUPPORTED, k, -1, "FP64 fused blocks are limited to k <= 5");
+    if (use_tc && d_tc && s->prec == QI_F32 && k >= 5 && n >= k + 7) return launch_fused_tc(s, k, targets, d_tc);
+    return launch_fused_simt(s, k, targets, d_mat);
 }
 
 Status launch_diagk(qi_state *s, int k, const int32_t *targets, const void *d_phases) {
     if (k < 1 || k > 10) return err(QI_ERR_INVALID_INPUT_VALUE, k, -1, "diagonal block width");
-    uint64_t tmask = 0;
-    for (int j = 0; j < k; ++j) tmask |= 1ull << targets[j];
-    uint64_t g = (s->dim() + 255) / 256;
+    DiagParams p;
+    std::memset(&p, 0, sizeof(p));
+    p.k = k;
+    for (int j = 0; j < k; ++j) p.pos[j] = (int8_t)targets[j];
+    const bool f32 = s->prec == QI_F32;
+    p.nvec = f32 ? (s->dim() >> 1) : s->dim();
+    if (f32 && s->n < 1) return err(QI_ERR_INVALID_NUMBER_OF_QUBITS, s->n);
+    uint64_t g = (p.nvec + 256ull * kDiagUnroll - 1) / (256ull * kDiagUnroll);
+    if (g < 1) g = 1;
     if (g > 152 * 8) g = 152 * 8;
-    if (s->prec == QI_F32)
-        k_diagk<float><<<(unsigned)g, 256, 0, s->stream>>>((float2 *)s->amps, s->dim(), (const float2 *)d_phases, k, tmask);
-    else
-        k_diagk<double><<<(unsigned)g, 256, 0, s->stream>>>((double2 *)s->amps, s->dim(), (const double2 *)d_phases, k,
-                                                           tmask);
+    if (f32) k_diagk<float><<<(unsigned)g, 256, 0, s->stream>>>((float2 *)s->amps, (const float2 *)d_phases, p);
+    else k_diagk<double><<<(unsigned)g, 256, 0, s->stream>>>((double2 *)s->amps, (const double2 *)d_phases, p);
     count_launch();
     return check_launch("k_diagk");
 }

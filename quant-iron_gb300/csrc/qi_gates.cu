@@ -490,7 +490,7 @@ static void launch_mat1_t(typename Cx<T>::V2 *a, const GateParams &p, int mode, 
 #undef QI_M1
 }
 
-Status launch_op(qi_state *s, const Op &op, const void *d_mats) {
+Status launch_op(qi_state *s, const Op &op, const void *d_mats, const void *d_tc) {
     const int n = s->n;
     const bool f32 = s->prec == QI_F32;
     GateParams p;
@@ -555,8 +555,11 @@ Status launch_op(qi_state *s, const Op &op, const void *d_mats) {
     case OP_FUSED: {
         const size_t esz = f32 ? sizeof(float2) : sizeof(double2);
         const char *mp = (const char *)d_mats + (size_t)op.mat_offset * esz;
-        return launch_fused(s, op.k, op.targets, mp, op.mode);
+        const void *tp = (d_tc && op.tc_offset >= 0) ? (const void *)((const float *)d_tc + op.tc_offset) : nullptr;
+        return launch_fused(s, op.k, op.targets, mp, tp, op.mode);
     }
+    case OP_NORMALISE:
+        return state_normalise_device_async(s);
     case OP_DIAGK: {
         const size_t esz = f32 ? sizeof(float2) : sizeof(double2);
         const char *mp = (const char *)d_mats + (size_t)op.mat_offset * esz;

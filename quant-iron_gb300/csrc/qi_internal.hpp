@@ -90,6 +90,7 @@ enum OpKind : int32_t {
     OP_PAULI_EXP = 5,     // cosh(a) psi + sinh(a) P psi
     OP_PAULI_NORM = 6,    // P psi then normalise (Gate::PauliString)
     OP_DIAGK = 7,         // diagonal on k targets (2^k phases), controlled by nothing
+    OP_NORMALISE = 8,     // FP64 norm on the device, divide (periodic renormalisation)
 };
 enum Mat1Mode : int32_t { M1_GENERAL = 0, M1_DIAG = 1, M1_ANTIDIAG = 2, M1_PHASE1 = 3, M1_REAL = 4 };
 
@@ -101,6 +102,7 @@ struct Op {
     uint64_t cmask = 0;            // control mask (controls must be 1)
     double m[32] = {0};            // MAT1: 4 complex; MAT2: 16 complex (row-major re, im)
     int64_t mat_offset = -1;       // OP_FUSED / OP_DIAGK: offset (complex entries) into the plan's matrix buffer
+    int64_t tc_offset = -1;        // OP_FUSED: offset (floats) of the tensor-core operand blocks, -1 if none
     uint64_t xmask = 0, zmask = 0; // Pauli ops
     double alpha_re = 0, alpha_im = 0;   // Pauli exp: cosh/sinh coefficients are derived from this
     double cre = 0, cim = 0, sre = 0, sim = 0;
@@ -127,7 +129,7 @@ Status gate_to_matrix(int n, const qi_gate &g, GateMatrix *out);
 // Lower a GateMatrix to a single primitive op.
 Op lower_gate(int n, const GateMatrix &gm);
 // Launch one primitive op on the state's stream (no synchronisation).
-Status launch_op(qi_state *s, const Op &op, const void *d_mats);
+Status launch_op(qi_state *s, const Op &op, const void *d_mats, const void *d_tc = nullptr);
 
 // ------------------------------------------------------------------ pauli --
 Status launch_pauli_exp(qi_state *s, uint64_t xmask, uint64_t zmask, double cre, double cim, double sre, double sim);
@@ -137,7 +139,14 @@ Status validate_pauli(int n, const qi_pauli_term &t);
 // ------------------------------------------------------------------ fused --
 // Apply a dense 2^k x 2^k complex matrix (device pointer, row-major, element
 // type matches the state's precision) on sorted targets.
-Status launch_fused(qi_state *s, int k, const int32_t *targets, const void *d_mat, int use_tc);
+Status launch_fused(qi_state *s, int k, const int32_t *targets, const void *d_mat, const void *d_tc, int use_tc);
+// 3xTF32 tcgen05 kernel (FP32 states, k = 5 or 6, n >= k + 7); d_tc holds the
+// six operand blocks prepared by tc_blocks().
+Status launch_fused_tc(qi_state *s, int k, const int32_t *targets, const void *d_tc);
+// Host: the six K-major operand blocks {Re U, Im U, -Im U} x {tf32 hi, lo}
+// (each 2^k x 2^k floats in the no-swizzle core-matrix layout) of a fused
+// matrix U (row-major complex, FP64).  Appends 6 * 4^k floats to `out`.
+void tc_blocks(int k, const double *U, std::vector<float> &out);
 Status launch_diagk(qi_state *s, int k, const int32_t *targets, const void *d_phases);
 
 }  // namespace qi

@@ -203,6 +203,8 @@ Status build_plan(qi_plan *p, std::vector<Elem> &elems) {
     if (p->prec == QI_F64) kmax = std::min(kmax, 5);
     p->ops.clear();
     p->mats.clear();
+    p->tc.clear();
+    int tc_blocks_since = 0, tc_total = 0;
     std::fill(std::begin(p->stats.n_blocks_by_k), std::end(p->stats.n_blocks_by_k), 0);
     p->stats.n_gates = (int64_t)elems.size();
     // Pauli exponentials narrow enough become dense elements when fusing.
@@ -257,12 +259,33 @@ Status build_plan(qi_plan *p, std::vector<Elem> &elems) {
                 for (int r = 0; r < dim; ++r) p->mats.push_back(mb[bi][(size_t)r * dim + r]);
             } else {
                 op.kind = OP_FUSED;
-                op.mode = p->opts.use_tensor_cores;
+                op.mode = p->opts.use_tensor_cores != 2;
                 for (size_t i = 0; i < (size_t)dim * dim; ++i) p->mats.push_back(mb[bi][i]);
+                if (op.mode && p->prec == QI_F32 && k >= 5 && n >= k + 7) {
+                    op.tc_offset = (int64_t)p->tc.size();
+                    tc_blocks(k, reinterpret_cast<const double *>(mb[bi].data()), p->tc);
+                }
             }
             p->ops.push_back(op);
             p->stats.n_blocks_by_k[k]++;
+            if (op.tc_offset >= 0) {
+                ++tc_blocks_since;
+                ++tc_total;
+                if (p->opts.renorm_every > 0 && tc_blocks_since >= p->opts.renorm_every) {
+                    Op nrm;
+                    nrm.kind = OP_NORMALISE;
+                    p->ops.push_back(nrm);
+                    tc_blocks_since = 0;
+                }
+            }
         }
+    }
+    // Tensor-core accumulation rounds toward zero: renormalise once at the end
+    // (unless disabled, or the last op already did).
+    if (tc_total > 0 && p->opts.renorm_every >= 0 && (p->ops.empty() || p->ops.back().kind != OP_NORMALISE)) {
+        Op nrm;
+        nrm.kind = OP_NORMALISE;
+        p->ops.push_back(nrm);
     }
     p->stats.n_kernels = (int64_t)p->ops.size();
     return ok_status();
@@ -270,6 +293,11 @@ Status build_plan(qi_plan *p, std::vector<Elem> &elems) {
 
 Status upload_plan(qi_plan *p) {
     if (p->d_mats) { cudaFree(p->d_mats); p->d_mats = nullptr; }
+    if (p->d_tc) { cudaFree(p->d_tc); p->d_tc = nullptr; }
+    if (!p->tc.empty()) {
+        QI_CUDA(cudaMalloc(&p->d_tc, p->tc.size() * sizeof(float)));
+        QI_CUDA(cudaMemcpy(p->d_tc, p->tc.data(), p->tc.size() * sizeof(float), cudaMemcpyHostToDevice));
+    }
     if (p->mats.empty()) return ok_status();
     const size_t cnt = p->mats.size();
     if (p->prec == QI_F32) {
@@ -313,13 +341,13 @@ Status plan_elems_from_gates(int n, const qi_gate *gates, int64_t ng, const doub
 Status plan_execute(qi_plan *p, qi_state *s) {
     if (s->n != p->n) return err(QI_ERR_INVALID_NUMBER_OF_QUBITS, s->n);   // circuit.rs:161-163
     if (s->prec != p->prec) return err(QI_ERR_UNSUPPORTED, -1, -1, "plan precision differs from state");
-    if (!p->d_mats && !p->mats.empty()) {   // matrices go to the device on first use
+    if ((!p->d_mats && !p->mats.empty()) || (!p->d_tc && !p->tc.empty())) {   // matrices go to the device on first use
         Status up = upload_plan(p);
         if (!up.ok()) return up;
     }
     bool has_norm = false;
     for (const Op &op : p->ops) {
-        Status st = launch_op(s, op, p->d_mats);
+        Status st = launch_op(s, op, p->d_mats, p->d_tc);
         if (!st.ok()) return st;
         has_norm = has_norm || op.kind == OP_PAULI_NORM;
     }
@@ -389,7 +417,7 @@ qi_status qi_plan_profile(qi_plan *p, qi_state *s, float *ms_out) {
     cudaError_t e = cudaSetDevice(s->device);
     if (e != cudaSuccess) return publish(cuda_status(e, "cudaSetDevice"));
     if (s->n != p->n || s->prec != p->prec) return publish(err(QI_ERR_INVALID_NUMBER_OF_QUBITS, s->n));
-    if (!p->d_mats && !p->mats.empty()) {
+    if ((!p->d_mats && !p->mats.empty()) || (!p->d_tc && !p->tc.empty())) {
         Status up = upload_plan(p);
         if (!up.ok()) return publish(up);
     }
@@ -402,7 +430,7 @@ qi_status qi_plan_profile(qi_plan *p, qi_state *s, float *ms_out) {
     Status st = ok_status();
     cudaEventRecord(ev[0], s->stream);
     for (size_t i = 0; i < nops && st.ok(); ++i) {
-        st = launch_op(s, p->ops[i], p->d_mats);
+        st = launch_op(s, p->ops[i], p->d_mats, p->d_tc);
         cudaEventRecord(ev[i + 1], s->stream);
     }
     e = cudaStreamSynchronize(s->stream);
@@ -413,6 +441,68 @@ qi_status qi_plan_profile(qi_plan *p, qi_state *s, float *ms_out) {
         ms_out[i] = ms;
     }
     for (auto &x : ev) cudaEventDestroy(x);
+    return publish(st);
+}
+
+qi_status qi_apply_matrix(qi_state *s, const int32_t *targets, int32_t k, const double *matrix,
+                          int32_t use_tensor_cores) {
+    if (!s || !targets || !matrix) return publish(err(QI_ERR_NULL_ARGUMENT));
+    std::lock_guard<std::recursive_mutex> lk(s->mu);
+    cudaError_t e = cudaSetDevice(s->device);
+    if (e != cudaSuccess) return publish(cuda_status(e, "cudaSetDevice"));
+    if (k < 1 || k > 6) return publish(err(QI_ERR_INVALID_NUMBER_OF_QUBITS, k));
+    const int n = s->n;
+    for (int j = 0; j < k; ++j) {
+        if (targets[j] < 0 || targets[j] >= n) return publish(err(QI_ERR_INVALID_QUBIT_INDEX, targets[j], n));
+        for (int i = 0; i < j; ++i)
+            if (targets[i] == targets[j]) return publish(err(QI_ERR_INVALID_QUBIT_INDEX, targets[j], n));
+    }
+    // sort targets and permute the matrix to the sorted local order
+    std::vector<int> order(k);
+    for (int j = 0; j < k; ++j) order[j] = j;
+    std::sort(order.begin(), order.end(), [&](int x, int y) { return targets[x] < targets[y]; });
+    const int dim = 1 << k;
+    auto remap = [&](int idx) {   // sorted-local index -> caller-local index
+        int o = 0;
+        for (int j = 0; j < k; ++j) o |= ((idx >> j) & 1) << order[j];
+        return o;
+    };
+    std::vector<cd> U((size_t)dim * dim);
+    for (int r = 0; r < dim; ++r)
+        for (int c = 0; c < dim; ++c) {
+            const size_t src = (size_t)remap(r) * dim + remap(c);
+            U[(size_t)r * dim + c] = cd(matrix[2 * src], matrix[2 * src + 1]);
+        }
+    qi_plan plan;
+    plan.n = n;
+    plan.prec = s->prec;
+    Op op;
+    op.kind = OP_FUSED;
+    op.k = k;
+    for (int j = 0; j < k; ++j) op.targets[j] = targets[order[j]];
+    op.mat_offset = 0;
+    op.mode = use_tensor_cores != 2;
+    plan.mats = U;
+    if (op.mode && s->prec == QI_F32 && k >= 5 && n >= k + 7) {
+        op.tc_offset = 0;
+        tc_blocks(k, reinterpret_cast<const double *>(U.data()), plan.tc);
+    }
+    if (s->prec == QI_F64 && k > 5) return publish(err(QI_ERR_UNSUPPORTED, k, -1, "FP64 blocks are limited to k <= 5"));
+    plan.ops.push_back(op);
+    Status st = upload_plan(&plan);
+    if (st.ok()) st = plan_execute(&plan, s);
+    if (st.ok()) {
+        e = cudaStreamSynchronize(s->stream);
+        if (e != cudaSuccess) st = cuda_status(e, "apply_matrix");
+    }
+    if (st.ok()) {
+        int flag = 0;
+        st = state_read_flag(s, &flag);
+        if (st.ok() && flag == 2) st = err(QI_ERR_TIMEOUT, -1, -1, "tensor-core kernel wait timed out");
+    }
+    if (plan.d_mats) cudaFree(plan.d_mats);
+    if (plan.d_tc) cudaFree(plan.d_tc);
+    plan.d_mats = plan.d_tc = nullptr;
     return publish(st);
 }
 
@@ -430,6 +520,7 @@ qi_status qi_plan_op_get(const qi_plan *p, int64_t i, qi_plan_op_info *info, dou
     info->kind = op.kind;
     info->k = op.k;
     for (int j = 0; j < 6; ++j) info->targets[j] = op.targets[j];
+    info->tensor_cores = (op.kind == OP_FUSED && op.tc_offset >= 0) ? 1 : 0;
     info->control_mask = op.cmask;
     info->xmask = op.xmask;
     info->zmask = op.zmask;
@@ -460,6 +551,7 @@ qi_status qi_plan_op_get(const qi_plan *p, int64_t i, qi_plan_op_info *info, dou
 qi_status qi_plan_destroy(qi_plan *p) {
     if (!p) return QI_OK;
     if (p->d_mats) cudaFree(p->d_mats);
+    if (p->d_tc) cudaFree(p->d_tc);
     delete p;
     return QI_OK;
 }
@@ -474,7 +566,14 @@ qi_status qi_circuit_execute(qi_state *s, const qi_gate *gates, int64_t n_gates,
     if (st == QI_OK) {
         std::lock_guard<std::recursive_mutex> lk(s->mu);
         cudaError_t e = cudaStreamSynchronize(s->stream);
-        if (e != cudaSuccess) st = publish(cuda_status(e, "execute"));
+        if (e != cudaSuccess) {
+            st = publish(cuda_status(e, "execute"));
+        } else {
+            int flag = 0;
+            Status fs = state_read_flag(s, &flag);
+            if (!fs.ok()) st = publish(fs);
+            else if (flag == 2) st = publish(err(QI_ERR_TIMEOUT, -1, -1, "tensor-core kernel wait timed out"));
+        }
     }
     qi_plan_destroy(p);
     return st;
@@ -525,6 +624,8 @@ qi_status qi_trotter_evolve(qi_state *s, const qi_pauli_term *terms, int64_t n_t
         }
     }
     if (plan.d_mats) cudaFree(plan.d_mats);
+    if (plan.d_tc) cudaFree(plan.d_tc);
+    plan.d_tc = nullptr;
     plan.d_mats = nullptr;
     if (!st.ok()) return publish(st);
     e = cudaStreamSynchronize(s->stream);

@@ -37,6 +37,8 @@ struct qi_plan {
     std::vector<qi::Op> ops;
     std::vector<std::complex<double>> mats;   // block matrices / phase tables (host copy, FP64)
     void *d_mats = nullptr;                   // same, in the plan's precision
+    std::vector<float> tc;                    // tensor-core operand blocks of FP32 fused ops (k >= 5)
+    void *d_tc = nullptr;
     qi_plan_stats stats = {};
     std::vector<qi::Block> partition_override;   // set by callers that chose the partition
 };

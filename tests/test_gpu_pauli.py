@@ -17,7 +17,7 @@ def rand_terms(n, count, seed, max_weight=3):
     rng = np.random.default_rng(seed)
     out = []
     for _ in range(count):
-        w = int(rng.integers(1, max_weight + 1))
+        w = int(rng.integers(1, min(max_weight, n) + 1))
         qs = rng.choice(n, w, replace=False)
         ops = [(int(q), "XYZ"[int(rng.integers(0, 3))]) for q in qs]
         out.append(workloads.term(complex(rng.uniform(-1, 1), rng.uniform(-1, 1) * (rng.random() < 0.3)), ops))

@@ -1,0 +1,129 @@
+"""Fused k-qubit blocks on the tensor cores (tcgen05, 3xTF32) vs numpy FP64 (GPU).
+
+Tolerance: the 3xTF32 products keep ~22 significant bits, so one block on a
+normalised random state stays within 2e-6 per amplitude of the FP64 result
+and its infidelity below 1e-10."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def haar(k, seed):
+    rng = np.random.default_rng(seed)
+    z = (rng.normal(size=(1 << k, 1 << k)) + 1j * rng.normal(size=(1 << k, 1 << k))) / np.sqrt(2)
+    q, r = np.linalg.qr(z)
+    return q * (np.diag(r) / np.abs(np.diag(r)))
+
+
+def apply_np(state, n, targets, U):
+    k = len(targets)
+    psi = state.reshape([2] * n)
+    axes = [n - 1 - t for t in targets[::-1]]
+    rest = [a for a in range(n) if a not in axes]
+    perm = axes + rest
+    t = np.transpose(psi, perm).reshape(1 << k, -1)
+    out = (U @ t).reshape([2] * n)
+    return np.transpose(out, np.argsort(perm)).reshape(-1)
+
+
+def rand_state(n, seed):
+    rng = np.random.default_rng(seed)
+    v = rng.normal(size=1 << n) + 1j * rng.normal(size=1 << n)
+    return v / np.linalg.norm(v)
+
+
+TARGET_SETS = {
+    6: [[0, 1, 2, 3, 4, 5], [7, 8, 9, 10, 11, 12], [0, 2, 5, 8, 11, 12], [1, 3, 4, 6, 9, 10], [0, 6, 7, 8, 9, 12]],
+    5: [[0, 1, 2, 3, 4], [8, 9, 10, 11, 12], [0, 3, 7, 10, 12], [2, 4, 5, 6, 11]],
+}
+
+
+@pytest.mark.parametrize("k", [5, 6])
+@pytest.mark.parametrize("n", [13, 14, 16])
+def test_tensor_core_block_vs_numpy(qi, k, n):
+    for i, targets in enumerate(TARGET_SETS[k]):
+        targets = [t if t < n else t - (13 - n) for t in targets]
+        U = haar(k, 10 * k + i)
+        init = rand_state(n, i)
+        want = apply_np(init, n, targets, U)
+        with qi.DeviceState(n, qi.F32) as st:
+            st.upload(init)
+            qi.apply_matrix(st, targets, U, use_tensor_cores=1)
+            got = st.download()
+        err = np.max(np.abs(got - want))
+        infid = 1 - abs(np.vdot(want, got)) ** 2 / np.vdot(got, got).real
+        assert err < 2e-6 and infid < 1e-10, (k, n, targets, err, infid)
+
+
+@pytest.mark.parametrize("k", [5, 6])
+def test_tensor_core_matches_cuda_core_path(qi, k):
+    n = 15
+    targets = [1, 4, 5, 9, 12, 14][:k]
+    U = haar(k, 3)
+    init = rand_state(n, 9)
+    outs = []
+    for tc in (1, 2):
+        with qi.DeviceState(n, qi.F32) as st:
+            st.upload(init)
+            qi.apply_matrix(st, targets, U, use_tensor_cores=tc)
+            outs.append(st.download())
+    assert np.max(np.abs(outs[0] - outs[1])) < 3e-6
+
+
+def test_unsorted_targets_and_small_states(qi):
+    # targets given out of order; n too small for the tensor-core tile falls back to CUDA cores
+    for n in (6, 9, 13):
+        targets = [3, 0, 5, 1, 4, 2] if n > 6 else [5, 0, 3, 1, 4, 2]
+        U = haar(6, n)
+        init = rand_state(n, n)
+        want = apply_np(init, n, targets, U)
+        with qi.DeviceState(n, qi.F32) as st:
+            st.upload(init)
+            qi.apply_matrix(st, targets, U)
+            assert np.max(np.abs(st.download() - want)) < 2e-6
+
+
+def test_circuit_fused_tensor_cores_vs_oracle(qi, orc):
+    from quant_iron_gb300 import workloads
+    n = 16
+    gates = workloads.random_circuit(n, layers=6, seed=21)
+    init = workloads.plus_state(n)
+    want = orc.execute(init, n, gates)
+    for k in (5, 6):
+        plan = qi.Plan(n, qi.F32, gates, fusion=qi.FUSION_GREEDY, max_block_qubits=k, use_tensor_cores=1)
+        with qi.DeviceState(n, qi.F32) as st:
+            st.upload(init)
+            plan.execute(st)
+            got = st.download()
+        # renormalised at the end of the plan: both the raw overlap and the
+        # normalised infidelity are within the headline bound
+        assert abs(np.vdot(got, got).real - 1.0) < 1e-6
+        assert np.max(np.abs(got - want)) < 5e-6
+        assert 1 - abs(np.vdot(want, got)) ** 2 < 1e-6
+
+
+def test_tensor_core_norm_drift_and_renormalisation(qi):
+    """The tensor cores accumulate FP32 with rounding toward zero, so repeated
+    blocks shrink the norm slightly; the plan's FP64 renormalisation removes it."""
+    from quant_iron_gb300.workloads import GateList
+    n = 14
+    gl = GateList()
+    rng = np.random.default_rng(4)
+    for layer in range(30):
+        for q in range(6):
+            gl.add("RY", [q], [], [rng.uniform(0, 6.28)])
+            gl.add("RZ", [q], [], [rng.uniform(0, 6.28)])
+        for q in range(5):
+            gl.add("CNOT", [q + 1], [q])
+    gates = gl.array()
+    norms = {}
+    for renorm in (-1, 0, 5):
+        plan = qi.Plan(n, qi.F32, gates, fusion=qi.FUSION_GREEDY, max_block_qubits=6, use_tensor_cores=1,
+                       renorm_every=renorm)
+        with qi.DeviceState(n, qi.F32) as st:
+            st.set_plus()
+            plan.execute(st)
+            norms[renorm] = st.norm_sqr()
+    assert abs(norms[0] - 1.0) < 1e-6 and abs(norms[5] - 1.0) < 1e-6
+    assert abs(norms[-1] - 1.0) < 1e-3   # drift without renormalisation stays small

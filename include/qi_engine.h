@@ -275,6 +275,22 @@ qi_status qi_plan_create(int32_t num_qubits, int32_t precision, const qi_gate *g
 qi_status qi_plan_execute(qi_plan *p, qi_state *s);
 qi_status qi_plan_stats_get(const qi_plan *p, qi_plan_stats *out);
 qi_status qi_plan_destroy(qi_plan *p);
+/* Adjoint (reverse-mode) gradient of E(theta) = <psi(theta)|H|psi(theta)> with
+ * psi(theta) = U_N(theta) ... U_1(theta) |psi0> and H = sum of `terms` (a
+ * SumOp, pauli_string.rs:390-507).  No reference counterpart: it sits beside
+ * Circuit::execute (circuit.rs:160-172) and differentiates through the
+ * parametric gates (parametric_gate.rs:30-211, Parameter::get parameter.rs:52-57).
+ * One forward sweep (fused plan), lambda = H psi, then one reverse sweep in
+ * which each gate is un-applied to psi and lambda in a single pass that also
+ * accumulates 2 Re<lambda|dU/dtheta|psi> in FP64.  Differentiable kinds: RX,
+ * RY, RZ, P, RYPHASE, RYPHASE_DAG, MATCHGATE (any controls).
+ * On entry `s` holds |psi0>; on return it holds |psi0> again (restored by the
+ * reverse sweep up to rounding).  energy_out (may be NULL) receives E;
+ * grads_out[j] = dE/dtheta_j for j < n_theta (parameters that no gate uses get 0). */
+qi_status qi_adjoint_gradient(qi_state *s, const qi_gate *gates, int64_t n_gates, const double *theta,
+                              int64_t n_theta, const qi_pauli_term *terms, int64_t n_terms,
+                              const qi_exec_options *forward_opts, double *energy_out, double *grads_out);
+
 /* Inspect the i-th device operation of a plan (host only; no device work).
  * Lets tests check the fusion pass without a GPU. */
 typedef struct qi_plan_op_info {

@@ -313,3 +313,19 @@ def apply_matrix(state, targets, matrix, use_tensor_cores=0):
     m = np.ascontiguousarray(matrix, dtype=np.complex128).reshape(-1).view(np.float64)
     check(lib.qi_apply_matrix(state.h, t.ctypes.data, t.size, m.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
                               int(use_tensor_cores)))
+
+
+def adjoint_gradient(state, gates, theta, terms, fusion=FUSION_GREEDY, max_block_qubits=0, use_tensor_cores=0):
+    """dE/dtheta of E = <psi(theta)|H|psi(theta)> by one forward and one reverse sweep.
+    `state` holds |psi0> before and after the call.  Returns (E, grads)."""
+    gates = np.ascontiguousarray(gates, dtype=GATE_DTYPE)
+    t = np.ascontiguousarray(theta, dtype=np.float64)
+    h = _terms(terms)
+    grads = np.zeros(t.size, dtype=np.float64)
+    energy = ctypes.c_double()
+    opts = _options(fusion, max_block_qubits, use_tensor_cores)
+    pd = ctypes.POINTER(ctypes.c_double)
+    check(lib.qi_adjoint_gradient(state.h, gates.ctypes.data if gates.size else None, gates.size, t.ctypes.data_as(pd),
+                                  t.size, h.ctypes.data if h.size else None, h.size, ctypes.byref(opts),
+                                  ctypes.byref(energy), grads.ctypes.data_as(pd)))
+    return energy.value, grads

@@ -14,12 +14,13 @@
 // A_hi B_hi + A_hi B_lo + A_lo B_hi are accumulated in FP32, which keeps
 // about 22 significant bits (the dropped A_lo B_lo term is ~2^-22 relative).
 //
-// Per tile (one CTA per SM, persistent):
-//   cp.async load of tile t+1 in flight (qi_tile.cuh, [row][column] layout)
-//   8 warps read the tile, split hi/lo and tcgen05.st A_hi / A_lo to TMEM
+// Per tile (one CTA of 16 warps per SM, persistent):
+//   16 warps read the tile (qi_tile.cuh, [row][column] layout), split hi/lo
+//   and tcgen05.st A_hi / A_lo to TMEM (warp w: lanes 32*(w%4).., rows slice w/4)
 //   one thread issues the 6 * 2R/8 MMAs (M128 x N=R x K8) and commits to an
 //   mbarrier; every wait on it is bounded and a timeout sets the error flag
-//   8 warps tcgen05.ld D, write OUT into the tile buffer, then store it.
+//   while the MMAs run: store tile t-1's output, cp.async-prefetch tile t+1
+//   16 warps tcgen05.ld D and write OUT into the tile buffer.
 // Tensor-memory columns: A_hi [0, 2R), A_lo [2R, 4R), D_re [4R, 5R), D_im [5R, 6R).
 #include "qi_internal.hpp"
 #include "qi_device.cuh"
@@ -30,7 +31,7 @@
 
 namespace qi {
 
-constexpr int kTcThreads = 256;
+constexpr int kTcThreads = 512;   // 16 warps: 4 lane quarters x 4 row slices
 constexpr uint32_t kWaitLimit = 1u << 22;   // bounded mbarrier wait (iterations of try_wait)
 
 // ---------------------------------------------------------- PTX wrappers --
@@ -115,6 +116,12 @@ __device__ __forceinline__ uint32_t tf32_rna(float x) {
 template <int N>
 __device__ __forceinline__ void tmem_st(uint32_t taddr, const uint32_t (&v)[N]);
 template <>
+__device__ __forceinline__ void tmem_st<8>(uint32_t taddr, const uint32_t (&v)[8]) {
+    asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};\n" ::"r"(taddr),
+                 "r"(v[0]), "r"(v[1]), "r"(v[2]), "r"(v[3]), "r"(v[4]), "r"(v[5]), "r"(v[6]), "r"(v[7])
+                 : "memory");
+}
+template <>
 __device__ __forceinline__ void tmem_st<16>(uint32_t taddr, const uint32_t (&v)[16]) {
     asm volatile(
         "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
@@ -136,6 +143,13 @@ __device__ __forceinline__ void tmem_st<32>(uint32_t taddr, const uint32_t (&v)[
 }
 template <int N>
 __device__ __forceinline__ void tmem_ld(uint32_t taddr, uint32_t (&v)[N]);
+template <>
+__device__ __forceinline__ void tmem_ld<8>(uint32_t taddr, uint32_t (&v)[8]) {
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];\n"
+                 : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7])
+                 : "r"(taddr)
+                 : "memory");
+}
 template <>
 __device__ __forceinline__ void tmem_ld<16>(uint32_t taddr, uint32_t (&v)[16]) {
     asm volatile(
@@ -166,7 +180,7 @@ template <int K>
 struct TcCfg {
     static constexpr int R = 1 << K;            // rows (target patterns)
     static constexpr int KR = 2 * R;            // real K of the GEMM
-    static constexpr int H = R / 2;             // rows per warp half
+    static constexpr int H = R / 4;             // rows per warp slice
     static constexpr int BLK = R * R;           // floats per operand block
     static constexpr uint32_t LBO = 128;        // next core matrix along K
     static constexpr uint32_t SBO = (R / 4) * 128;   // next 8-row group along N
@@ -191,7 +205,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_fused_tc(float2 *a, const flo
     volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int quarter = warp & 3, half = warp >> 2;
+    const int quarter = warp & 3, half = warp >> 2;   // lane quarter, row slice (0..3)
 
     // operand blocks -> shared memory (16-byte vectors), visible to the async proxy
     {
@@ -215,15 +229,24 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_fused_tc(float2 *a, const flo
     const uint32_t lane_base = (uint32_t)(quarter * 32) << 16;
     const int m = quarter * 32 + lane;   // this thread's tile column / TMEM lane
 
+    // Descriptor of block 0 at K offset 0; every MMA adds a constant byte offset
+    // (>> 4 into the start-address field, which cannot carry: blocks stay below 256 KB).
+    const uint64_t desc0 = smem_desc(smem_u32(sB), C::LBO, C::SBO);
+    const uint32_t idesc = tf32_idesc(128, R);
+
+    // Software pipeline over this CTA's tiles (buffers alternate):
+    //   wait tile t -> convert(t) -> issue MMA(t) -> store output of tile t-1 and
+    //   prefetch tile t+1 into its buffer while the MMAs run -> wait -> epilogue(t)
     uint64_t t = blockIdx.x;
     if (t < g.ntiles) tile_load_async(g, w, tab, a, tile_base(g, t), S0);
     cp_async_commit();
-    if (t + gridDim.x < g.ntiles) tile_load_async(g, w, tab, a, tile_base(g, t + gridDim.x), S1);
-    cp_async_commit();
 
-    for (int it = 0; t < g.ntiles; ++it, t += gridDim.x) {
+    uint64_t prev_t = 0;
+    int it = 0;
+    for (; t < g.ntiles; ++it, t += gridDim.x) {
         float2 *S = (it & 1) ? S1 : S0;
-        cp_async_wait<1>();
+        float2 *Sprev = (it & 1) ? S0 : S1;
+        cp_async_wait<0>();
         __syncthreads();
         if (*abort_flag) break;
 
@@ -258,28 +281,34 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_fused_tc(float2 *a, const flo
         // ---- MMA: one thread issues all products, commits to the mbarrier
         if (tid == 0) {
             tc_fence_after();
-            const uint32_t idesc = tf32_idesc(128, R);
-            const uint32_t sb = smem_u32(sB);
             // block order in shared memory: 0 Re hi, 1 Im hi, 2 -Im hi, 3 Re lo, 4 Im lo, 5 -Im lo
+#pragma unroll
             for (int part = 0; part < 2; ++part) {
                 const uint32_t d = tmem + C::COL_D + part * R;
-                uint32_t acc = 0;
+#pragma unroll
                 for (int prod = 0; prod < 3; ++prod) {
                     const uint32_t acol = (prod == 2) ? C::COL_ALO : C::COL_AHI;   // A_hi, A_hi, A_lo
                     const int bset = (prod == 1) ? 3 : 0;                          // B_hi, B_lo, B_hi
+#pragma unroll
                     for (int j = 0; j < C::KR / 8; ++j) {
                         const int kk = 8 * j;
                         const bool first_half = kk < R;
                         const int blk = part == 0 ? (first_half ? 0 : 2) : (first_half ? 1 : 0);
                         const int koff = first_half ? kk : kk - R;
-                        const uint32_t baddr = sb + (uint32_t)((bset + blk) * C::BLK * 4) + (uint32_t)(koff / 4) * C::LBO;
-                        mma_tf32_ts(d, tmem + acol + kk, smem_desc(baddr, C::LBO, C::SBO), idesc, acc);
-                        acc = 1;
+                        const uint32_t boff = (uint32_t)((bset + blk) * C::BLK * 4) + (uint32_t)(koff / 4) * C::LBO;
+                        mma_tf32_ts(d, tmem + acol + kk, desc0 + (uint64_t)(boff >> 4), idesc,
+                                    (prod == 0 && j == 0) ? 0u : 1u);
                     }
                 }
             }
             mma_commit(mbar);
         }
+        // ---- while the tensor cores run: store tile t-1's output, prefetch tile t+1
+        if (it > 0) tile_store(g, w, tab, a, tile_base(g, prev_t), Sprev);
+        __syncthreads();
+        const uint64_t nt = t + gridDim.x;
+        if (nt < g.ntiles) tile_load_async(g, w, tab, a, tile_base(g, nt), Sprev);
+        cp_async_commit();
         // ---- wait for the products (bounded)
         if (!mbar_wait_bounded(mbar, (uint32_t)(it & 1))) {
             *abort_flag = 1;
@@ -301,14 +330,12 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_fused_tc(float2 *a, const flo
                 S[tile_sidx(g, n0 + i, m)] = make_float2(__uint_as_float(dr[i]), __uint_as_float(di[i]));
         }
         tc_fence_before();
-        __syncthreads();
-        tile_store(g, w, tab, a, tile_base(g, t), S);
-        __syncthreads();
-        const uint64_t nt = t + 2ull * gridDim.x;
-        if (nt < g.ntiles) tile_load_async(g, w, tab, a, tile_base(g, nt), S);
-        cp_async_commit();
+        prev_t = t;
     }
     cp_async_wait<0>();
+    __syncthreads();
+    // output of the last tile (skipped if the loop stopped on a timeout)
+    if (it > 0 && !*abort_flag) tile_store(g, w, tab, a, tile_base(g, prev_t), ((it - 1) & 1) ? S1 : S0);
     tc_fence_before();
     __syncthreads();
     if (warp == 0) {

@@ -1,0 +1,113 @@
+"""Adjoint gradient vs FP64 central finite differences and parameter shift (GPU).
+
+Norm-wise relative error ||g - g_ref|| / ||g_ref||: <= 1e-6 with an FP64
+state (the benchmark spec's bound), <= 1e-4 with an FP32 state (FP32 rounding of
+~1e3 gate applications); finite differences use eps = 1e-4 on the FP64 oracle."""
+import numpy as np
+import pytest
+
+from quant_iron_gb300 import workloads
+
+pytestmark = pytest.mark.gpu
+
+
+def energy_oracle(orc, n, gates, theta, terms, init):
+    return orc.sumop_expectation(orc.execute(init, n, gates, theta=theta), n, terms).real
+
+
+def fd_grad(orc, n, gates, theta, terms, init, ids, eps=1e-4):
+    g = np.zeros(len(ids))
+    for i, j in enumerate(ids):
+        tp, tm = theta.copy(), theta.copy()
+        tp[j] += eps
+        tm[j] -= eps
+        g[i] = (energy_oracle(orc, n, gates, tp, terms, init) - energy_oracle(orc, n, gates, tm, terms, init)) / (2 * eps)
+    return g
+
+
+@pytest.mark.parametrize("prec,tol", [(0, 1e-6), (1, 1e-4)], ids=["f64", "f32"])
+def test_hea_gradient_vs_finite_differences(qi, orc, prec, tol):
+    n = 8
+    gates, theta = workloads.hea_ansatz(n, layers=3, seed=1)
+    terms = workloads.xxz_periodic(n, seed=1)
+    init = workloads.zero_state(n)
+    with qi.DeviceState(n, prec) as st:
+        st.upload(init)
+        e, g = qi.adjoint_gradient(st, gates, theta, terms)
+        back = st.download()
+    e_ref = energy_oracle(orc, n, gates, theta, terms, init)
+    assert abs(e - e_ref) < (1e-12 if prec == 0 else 1e-5)
+    ids = list(range(theta.size))
+    g_ref = fd_grad(orc, n, gates, theta, terms, init, ids)
+    rel = np.linalg.norm(g - g_ref) / np.linalg.norm(g_ref)
+    assert rel < tol, rel
+    # the reverse sweep restores the initial state
+    assert np.max(np.abs(back - init)) < (1e-12 if prec == 0 else 1e-5)
+
+
+def test_parameter_shift_rotations(qi, orc):
+    """RY/RZ: dE/dtheta = (E(theta + pi/2) - E(theta - pi/2)) / 2 exactly."""
+    n = 7
+    gates, theta = workloads.hea_ansatz(n, layers=2, seed=3)
+    terms = workloads.heisenberg_open_chain(n, seed=2)
+    init = workloads.zero_state(n)
+    with qi.DeviceState(n, 0) as st:
+        st.upload(init)
+        _, g = qi.adjoint_gradient(st, gates, theta, terms)
+    rng = np.random.default_rng(0)
+    for j in rng.choice(theta.size, 8, replace=False):
+        tp, tm = theta.copy(), theta.copy()
+        tp[j] += np.pi / 2
+        tm[j] -= np.pi / 2
+        ps = (energy_oracle(orc, n, gates, tp, terms, init) - energy_oracle(orc, n, gates, tm, terms, init)) / 2
+        assert abs(g[j] - ps) < 1e-10
+
+
+def test_controlled_and_two_parameter_gates(qi, orc):
+    n = 6
+    gl = workloads.GateList()
+    rng = np.random.default_rng(7)
+    theta = rng.uniform(-3, 3, size=10)
+    gl.add("H", [0]).add("H", [3])
+    gl.add("RX", [1], [0], [0.0], [0])
+    gl.add("RYPHASE", [2], [], [0.0, 0.0], [1, 2])
+    gl.add("CNOT", [3], [2])
+    gl.add("P", [4], [3, 1], [0.0], [3])
+    gl.add("MATCHGATE", [4], [], [0.0, 0.0, 0.0], [4, 5, 6])
+    gl.add("RYPHASE_DAG", [0], [5], [0.0, 0.0], [7, 8])
+    gl.add("RZ", [5], [], [0.0], [9])
+    gl.add("RX", [2], [], [0.0], [0])   # parameter 0 used twice
+    gates = gl.array()
+    terms = workloads.heisenberg_open_chain(n, seed=4)
+    init = workloads.plus_state(n)
+    with qi.DeviceState(n, 0) as st:
+        st.upload(init)
+        _, g = qi.adjoint_gradient(st, gates, theta, terms)
+    g_ref = fd_grad(orc, n, gates, theta, terms, init, list(range(theta.size)))
+    assert np.linalg.norm(g - g_ref) / np.linalg.norm(g_ref) < 1e-7
+
+
+def test_adjoint_rejects_non_differentiable(qi):
+    gl = workloads.GateList().add("H", [0], [], [], [0])
+    with qi.DeviceState(2, 0) as st:
+        st.set_zero()
+        with pytest.raises(qi.QuantIronError) as ei:
+            qi.adjoint_gradient(st, gl.array(), np.zeros(1), workloads.heisenberg_open_chain(2))
+        assert ei.value.variant == "Unsupported"
+
+
+def test_adjoint_26q_fp32_vs_fp64_gpu(qi):
+    """Config-3 shape (26 qubits, 12 layers, 624 parameters): FP32 adjoint vs FP64 adjoint
+    on the GPU (norm-wise relative difference), and a finite-difference spot check in FP64."""
+    n = 26
+    gates, theta = workloads.hea_ansatz(n, layers=12, seed=1)
+    terms = workloads.xxz_periodic(n, seed=1)
+    grads = {}
+    for prec in (0, 1):
+        with qi.DeviceState(n, prec) as st:
+            st.set_zero()
+            e, g = qi.adjoint_gradient(st, gates, theta, terms)
+            grads[prec] = (e, g)
+    rel = np.linalg.norm(grads[1][1] - grads[0][1]) / np.linalg.norm(grads[0][1])
+    assert rel < 1e-4, rel
+    assert abs(grads[1][0] - grads[0][0]) < 1e-4

@@ -229,6 +229,24 @@ qi_status qi_sumop_apply(qi_state *out, qi_state *in, const qi_pauli_term *terms
 /* out = sum_k <s|c_k P_k|s>            SumOp::expectation_value       pauli_string.rs:485-507 */
 qi_status qi_sumop_expectation(qi_state *s, const qi_pauli_term *terms, int64_t n_terms, double out[2]);
 
+/* <s|H|s> for H = sum of `terms`, on caller-owned device amplitudes
+ * (2^num_qubits float2 or double2 at `amps`), allocating no device memory.
+ * It has no counterpart in the reference.  It exists for callers that cannot
+ * call cudaMalloc where they evaluate energies — a host application whose GPU
+ * memory is owned by its own pool, or a tight solver loop that must not add
+ * the device-wide synchronisation of an allocation.  All temporaries live in
+ * one static device array of 137,472 bytes that every GPU loading this
+ * library holds until exit.  Limits: n_terms <= 4096, and at most 2048 terms
+ * sharing one X mask (else InvalidInputValue).  The first call on a device
+ * looks up that array's device address (cudaGetSymbolAddress) with the device
+ * current; make that first call before any stream capture.  All calls share
+ * the array: calls whose work overlaps on the GPU (other streams, other host
+ * threads) race.  Work is issued on `cuda_stream` (NULL = legacy default
+ * stream) and the call returns after it completes. */
+qi_status qi_sumop_expectation_noalloc(const void *amps, int32_t num_qubits, int32_t precision,
+                                       const qi_pauli_term *terms, int64_t n_terms, void *cuda_stream,
+                                       double out[2]);
+
 /* Trotter evolution (src/algorithms/time_evolution.rs:45-166).  order 1 =
  * first_order_trotter_step, 2 = second_order_trotter_step.  If observable !=
  * NULL and observe_every > 0, <observable> is evaluated (FP64 reduction)

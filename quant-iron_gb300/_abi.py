@@ -177,5 +177,7 @@ lib.qi_plan_profile.restype = _i32
 lib.qi_plan_profile.argtypes = [_vp, _vp, ctypes.POINTER(ctypes.c_float)]
 lib.qi_apply_matrix.restype = _i32
 lib.qi_apply_matrix.argtypes = [_vp, _vp, _i32, _pd, _i32]
+lib.qi_sumop_expectation_noalloc.restype = _i32
+lib.qi_sumop_expectation_noalloc.argtypes = [_vp, _i32, _i32, _vp, _i64, _vp, _pd]
 lib.qi_adjoint_gradient.restype = _i32
 lib.qi_adjoint_gradient.argtypes = [_vp, _vp, _i64, _pd, _i64, _vp, _i64, ctypes.POINTER(ExecOptions), _pd, _pd]

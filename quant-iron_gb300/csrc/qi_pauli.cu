@@ -495,3 +495,133 @@ qi_status qi_sumop_expectation(qi_state *s, const qi_pauli_term *terms, int64_t 
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// SumOp expectation without device allocation.
+//
+// For callers that cannot allocate GPU memory at the point of the call — a
+// host application that has handed the whole device to its own memory pool,
+// or a solver loop that must not insert the device-wide synchronisation that
+// cudaMalloc/cudaFree imply — this entry point reads the caller's amplitude
+// buffer and keeps all of its temporaries (per-block partial sums, the
+// accumulated result and the grouped term table) in one fixed, statically
+// allocated device array, kNoAllocScratchBytes bytes per GPU that loads the
+// library, held until process exit.  Limits: at most kNoAllocMaxTerms terms,
+// and at most kNoAllocMaxGroupTerms terms sharing one X mask.
+// Every call reuses the same array: two calls whose work overlaps on the GPU
+// (different streams, or different host threads) race on it.
+// ---------------------------------------------------------------------------
+namespace qi {
+
+constexpr int kNoAllocMaxTerms = 4096;
+constexpr int kNoAllocMaxGroupTerms = 2048;   // 48 KB of shared memory per group kernel
+constexpr size_t kNoAllocPartialsOff = 0;
+constexpr size_t kNoAllocResultOff = (size_t)kReduceBlocks * 4 * sizeof(double);        // 38912, 256-aligned
+constexpr size_t kNoAllocTermsOff = kNoAllocResultOff + 256;
+constexpr size_t kNoAllocScratchBytes = kNoAllocTermsOff + (size_t)kNoAllocMaxTerms * sizeof(GroupTerm);   // 137472
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+static std::mutex g_noalloc_mu;
+static void *g_noalloc_ptr[64] = {nullptr};   // device address of g_noalloc_scratch, per device ordinal
+
+// Device address of the scratch array on the current device (set-up on the
+// first call per device: cudaGetSymbolAddress with that device current).
+static Status noalloc_scratch(void **out) {
+    int dev = 0;
+    QI_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) return err(QI_ERR_UNSUPPORTED, dev, -1, "device ordinal above 63");
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+        void *p = nullptr;
+        QI_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+        g_noalloc_ptr[dev] = p;
+    }
+    *out = g_noalloc_ptr[dev];
+    return ok_status();
+}
+
+}  // namespace qi
+
+extern "C" qi_status qi_sumop_expectation_noalloc(const void *amps, int32_t num_qubits, int32_t precision,
+                                                  const qi_pauli_term *terms, int64_t n_terms, void *cuda_stream,
+                                                  double out[2]) {
+    if (!amps || !out || (!terms && n_terms > 0)) return publish(err(QI_ERR_NULL_ARGUMENT));
+    if (num_qubits <= 0 || num_qubits > 40) return publish(err(QI_ERR_INVALID_NUMBER_OF_QUBITS, num_qubits));
+    if (precision != QI_F32 && precision != QI_F64) return publish(err(QI_ERR_INVALID_INPUT_VALUE, precision));
+    if (n_terms < 0 || n_terms > kNoAllocMaxTerms)
+        return publish(err(QI_ERR_INVALID_INPUT_VALUE, n_terms, kNoAllocMaxTerms,
+                           "qi_sumop_expectation_noalloc: at most 4096 terms (fixed scratch array)"));
+    out[0] = out[1] = 0.0;
+    if (n_terms == 0) return publish(ok_status());   // pauli_string.rs:486-489
+    for (int64_t k = 0; k < n_terms; ++k) {
+        Status st = validate_pauli(num_qubits, terms[k]);
+        if (!st.ok()) return publish(st);
+    }
+    // group by X mask into fixed host arrays (no heap)
+    static thread_local uint64_t gx[kNoAllocMaxTerms];
+    static thread_local int32_t gcount[kNoAllocMaxTerms], gfirst[kNoAllocMaxTerms], term_group[kNoAllocMaxTerms];
+    static thread_local GroupTerm packed[kNoAllocMaxTerms];
+    int ng = 0;
+    for (int64_t k = 0; k < n_terms; ++k) {
+        int gi = 0;
+        while (gi < ng && gx[gi] != terms[k].xmask) ++gi;
+        if (gi == ng) { gx[ng] = terms[k].xmask; gcount[ng] = 0; ++ng; }
+        term_group[k] = gi;
+        ++gcount[gi];
+    }
+    for (int gi = 0, off = 0; gi < ng; ++gi) {
+        if (gcount[gi] > kNoAllocMaxGroupTerms)
+            return publish(err(QI_ERR_INVALID_INPUT_VALUE, gcount[gi], kNoAllocMaxGroupTerms,
+                               "qi_sumop_expectation_noalloc: at most 2048 terms per X mask"));
+        gfirst[gi] = off;
+        off += gcount[gi];
+        gcount[gi] = 0;
+    }
+    for (int64_t k = 0; k < n_terms; ++k) {
+        const int gi = term_group[k];
+        double pr, pi;
+        minus_i_pow(__builtin_popcountll(terms[k].xmask & terms[k].zmask), pr, pi);
+        GroupTerm t;
+        t.zmask = terms[k].zmask;
+        t.re = terms[k].coeff_re * pr - terms[k].coeff_im * pi;
+        t.im = terms[k].coeff_re * pi + terms[k].coeff_im * pr;
+        packed[gfirst[gi] + gcount[gi]++] = t;
+    }
+    void *scratch = nullptr;
+    Status st = noalloc_scratch(&scratch);
+    if (!st.ok()) return publish(st);
+    cudaStream_t stream = (cudaStream_t)cuda_stream;
+    double *partials = (double *)((char *)scratch + kNoAllocPartialsOff);
+    double *result = (double *)((char *)scratch + kNoAllocResultOff);
+    GroupTerm *d_terms = (GroupTerm *)((char *)scratch + kNoAllocTermsOff);
+    cudaError_t e = cudaMemcpyAsync(d_terms, packed, (size_t)n_terms * sizeof(GroupTerm), cudaMemcpyHostToDevice, stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(result, 0, 2 * sizeof(double), stream);   // the accumulator starts at zero
+    if (e != cudaSuccess) return publish(cuda_status(e, "qi_sumop_expectation_noalloc"));
+    const uint64_t dim = 1ull << num_qubits;
+    for (int gi = 0; gi < ng; ++gi) {
+        GroupHdr h;
+        h.xmask = gx[gi];
+        h.first = gfirst[gi];
+        h.count = gcount[gi];
+        const uint64_t work = h.xmask ? (dim >> 1) : dim;
+        const unsigned nb = (unsigned)std::min<uint64_t>(std::max<uint64_t>((work + kReduceThreads - 1) / kReduceThreads, 1),
+                                                         kReduceBlocks);
+        const size_t sm = (size_t)h.count * sizeof(GroupTerm);
+        if (precision == QI_F32)
+            k_group_expect<float><<<nb, kReduceThreads, sm, stream>>>((const float2 *)amps, dim, h, d_terms, partials);
+        else
+            k_group_expect<double><<<nb, kReduceThreads, sm, stream>>>((const double2 *)amps, dim, h, d_terms, partials);
+        k_accumulate<<<1, 256, 0, stream>>>(partials, (int)nb, result);
+        count_launch(2);
+        st = check_launch("qi_sumop_expectation_noalloc");
+        if (!st.ok()) return publish(st);
+    }
+    double host_res[2] = {0.0, 0.0};
+    e = cudaMemcpyAsync(host_res, result, 2 * sizeof(double), cudaMemcpyDeviceToHost, stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+    if (e != cudaSuccess) return publish(cuda_status(e, "qi_sumop_expectation_noalloc"));
+    out[0] = host_res[0];
+    out[1] = host_res[1];
+    return publish(ok_status());
+}

@@ -309,6 +309,32 @@ qi_status qi_adjoint_gradient(qi_state *s, const qi_gate *gates, int64_t n_gates
                               int64_t n_theta, const qi_pauli_term *terms, int64_t n_terms,
                               const qi_exec_options *forward_opts, double *energy_out, double *grads_out);
 
+/* ------------------------------------------------------------------------ */
+/* Learned fusion cost model (no reference counterpart)                      */
+/* ------------------------------------------------------------------------ */
+/* An MLP (20 features -> 3 x 64 ReLU -> 1) predicting y = log(device ms per
+ * 2^28 amplitudes) of one device op (dense block on tensor or CUDA cores,
+ * diagonal block, per-gate kernel; features in quant-iron_gb300/csrc/qi_mlp.hpp).
+ * Trained on the GPU by the engine's own kernels; QI_FUSION_LEARNED plans use
+ * it to choose between one kernel per gate and greedy k (tensor cores on/off). */
+#define QI_COSTMODEL_FEATURES 20
+/* Time `count` seeded random device ops on num_qubits-qubit FP32 and FP64
+ * states with CUDA events: features_out[count][20], log_ms_out[count]. */
+qi_status qi_costmodel_collect(int32_t num_qubits, int64_t count, uint64_t seed, float *features_out,
+                               float *log_ms_out);
+/* Full-batch Adam on (X[n][16], Y[n]) from a seeded He initialisation; the
+ * trained model becomes the process-wide model.  loss_history[epochs] may be NULL. */
+qi_status qi_costmodel_train(const float *X, const float *Y, int64_t n, int32_t epochs, float lr, uint64_t seed,
+                             float *loss_history);
+qi_status qi_costmodel_predict(const float *X, int64_t n, float *y_out);
+/* MSE loss and its gradient w.r.t. the flat parameter vector, for the current parameters. */
+qi_status qi_costmodel_loss_and_gradient(const float *X, const float *Y, int64_t n, float *loss_out,
+                                         float *grad_out);
+qi_status qi_costmodel_init(uint64_t seed);
+qi_status qi_costmodel_num_params(int64_t *out);
+qi_status qi_costmodel_get_params(float *out, int64_t capacity, int32_t *trained);
+qi_status qi_costmodel_set_params(const float *in, int64_t count, int32_t trained);
+
 /* Inspect the i-th device operation of a plan (host only; no device work).
  * Lets tests check the fusion pass without a GPU. */
 typedef struct qi_plan_op_info {

@@ -177,6 +177,20 @@ lib.qi_plan_profile.restype = _i32
 lib.qi_plan_profile.argtypes = [_vp, _vp, ctypes.POINTER(ctypes.c_float)]
 lib.qi_apply_matrix.restype = _i32
 lib.qi_apply_matrix.argtypes = [_vp, _vp, _i32, _pd, _i32]
+_pf = ctypes.POINTER(ctypes.c_float)
+for _name, _args in {
+    "qi_costmodel_collect": [_i32, _i64, _u64, _pf, _pf],
+    "qi_costmodel_train": [_pf, _pf, _i64, _i32, ctypes.c_float, _u64, _pf],
+    "qi_costmodel_predict": [_pf, _i64, _pf],
+    "qi_costmodel_loss_and_gradient": [_pf, _pf, _i64, _pf, _pf],
+    "qi_costmodel_init": [_u64],
+    "qi_costmodel_num_params": [ctypes.POINTER(_i64)],
+    "qi_costmodel_get_params": [_pf, _i64, ctypes.POINTER(_i32)],
+    "qi_costmodel_set_params": [_pf, _i64, _i32],
+}.items():
+    getattr(lib, _name).restype = _i32
+    getattr(lib, _name).argtypes = _args
+COSTMODEL_FEATURES = 20
 lib.qi_sumop_expectation_noalloc.restype = _i32
 lib.qi_sumop_expectation_noalloc.argtypes = [_vp, _i32, _i32, _vp, _i64, _vp, _pd]
 lib.qi_adjoint_gradient.restype = _i32

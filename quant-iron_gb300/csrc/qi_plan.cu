@@ -197,16 +197,29 @@ void compose_block(const std::vector<Elem> &elems, const Block &b, std::vector<i
 // ------------------------------------------------------------------ plan ---
 Status build_plan(qi_plan *p, std::vector<Elem> &elems) {
     const int n = p->n;
-    const int fusion = p->opts.fusion;
+    int fusion = p->opts.fusion;
     int kmax = p->opts.max_block_qubits > 0 ? p->opts.max_block_qubits : 6;
     kmax = std::min(kmax, std::min(6, n));
     if (p->prec == QI_F64) kmax = std::min(kmax, 5);
+    int use_tc = p->opts.use_tensor_cores != 2;
     p->ops.clear();
     p->mats.clear();
     p->tc.clear();
     int tc_blocks_since = 0, tc_total = 0;
     std::fill(std::begin(p->stats.n_blocks_by_k), std::end(p->stats.n_blocks_by_k), 0);
     p->stats.n_gates = (int64_t)elems.size();
+    p->stats.predicted_us = 0.0;
+    if (fusion == QI_FUSION_LEARNED && p->partition_override.empty()) {
+        // the cost model picks per-gate vs greedy k (and tensor cores); greedy k = kmax without a model
+        int kbest = kmax, tcbest = use_tc;
+        double ms = 0.0;
+        if (learned_choice(p, elems, kmax, &kbest, &tcbest, &ms)) {
+            p->stats.predicted_us = ms * 1e3;
+            if (kbest <= 1) fusion = QI_FUSION_NONE;
+            kmax = std::max(2, kbest);
+            use_tc = tcbest;
+        }
+    }
     // Pauli exponentials narrow enough become dense elements when fusing.
     for (Elem &e : elems) {
         if (e.pauli && !e.gm.normalise_after && fusion != QI_FUSION_NONE && __builtin_popcountll(e.mask) <= kmax)
@@ -259,7 +272,7 @@ Status build_plan(qi_plan *p, std::vector<Elem> &elems) {
                 for (int r = 0; r < dim; ++r) p->mats.push_back(mb[bi][(size_t)r * dim + r]);
             } else {
                 op.kind = OP_FUSED;
-                op.mode = p->opts.use_tensor_cores != 2;
+                op.mode = use_tc;
                 for (size_t i = 0; i < (size_t)dim * dim; ++i) p->mats.push_back(mb[bi][i]);
                 if (op.mode && p->prec == QI_F32 && k >= 5 && n >= k + 7) {
                     op.tc_offset = (int64_t)p->tc.size();

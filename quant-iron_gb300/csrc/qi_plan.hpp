@@ -51,5 +51,8 @@ Status plan_elems_from_gates(int n, const qi_gate *gates, int64_t ng, const doub
                              std::vector<Elem> &elems);
 // Partition choice for QI_FUSION_GREEDY / QI_FUSION_LEARNED (qi_costmodel.cu).
 std::vector<Block> choose_partition(qi_plan *p, const std::vector<Elem> &elems, int kmax);
+// QI_FUSION_LEARNED: best (k, tensor cores) by the trained cost model (k = 1: one kernel per gate);
+// false when no trained model is loaded.  *ms_out = predicted device time of the chosen plan.
+bool learned_choice(qi_plan *p, const std::vector<Elem> &elems, int kmax, int *k_out, int *tc_out, double *ms_out);
 Elem pauli_exp_elem(const qi_pauli_term &t, double far, double fai, int src);
 }  // namespace qi

@@ -43,6 +43,8 @@ def parse():
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
     ap.add_argument("--qubits", type=int, default=N_QUBITS)
     ap.add_argument("--skip-baselines", action="store_true", help="skip FP64/FP32 per-gate and CPU legs")
+    ap.add_argument("--profile-case", default=None, choices=["fused26"],
+                    help="run a small fixed case for ncu captures instead of the benchmark")
     return ap.parse_args()
 
 
@@ -147,6 +149,54 @@ def cpu_baseline(n, gates, budget_s=25.0):
             "seconds_per_gate": per_gate}
 
 
+def adjoint_leg(qi, workloads, stream, torch, np, n=26, layers=12):
+    """Adjoint gradient of the 26-qubit hardware-efficient ansatz (12 layers of RY.RZ + CNOT
+    ladder, 624 parameters, seed 1) on the periodic XXZ energy: gradients/s with an FP32
+    state, agreement with the FP64-state adjoint, and FP64 central differences (eps 1e-4)
+    on 8 seeded parameters."""
+    gates, theta = workloads.hea_ansatz(n, layers, seed=1)
+    terms = workloads.xxz_periodic(n, seed=1)
+    s32 = qi.DeviceState(n, qi.F32)
+    s32.set_stream(stream.cuda_stream)
+    s32.set_zero()
+    qi.adjoint_gradient(s32, gates, theta, terms)   # warm-up
+    reps = 3
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        e32, g32 = qi.adjoint_gradient(s32, gates, theta, terms)
+    torch.cuda.synchronize()
+    t_adj = (time.perf_counter() - t0) / reps
+    s32.close()
+    s64 = qi.DeviceState(n, qi.F64)
+    s64.set_stream(stream.cuda_stream)
+    s64.set_zero()
+    e64, g64 = qi.adjoint_gradient(s64, gates, theta, terms)
+    rel32 = float(np.linalg.norm(g32 - g64) / np.linalg.norm(g64))
+    # FP64 central differences with the plain per-gate FP64 path
+    rng = np.random.default_rng(1)
+    ids = rng.choice(theta.size, 8, replace=False)
+    fd = []
+    for j in ids:
+        vals = []
+        for sgn in (1, -1):
+            th = theta.copy()
+            th[j] += sgn * 1e-4
+            s64.set_zero()
+            qi.Plan(n, qi.F64, gates, theta=th, fusion=qi.FUSION_NONE).execute(s64)
+            vals.append(qi.sumop_expectation(s64, terms).real)
+        fd.append((vals[0] - vals[1]) / 2e-4)
+    fd = np.array(fd)
+    rel_fd = float(np.linalg.norm(g64[ids] - fd) / np.linalg.norm(fd))
+    rel_fd32 = float(np.linalg.norm(g32[ids] - fd) / np.linalg.norm(fd))
+    s64.close()
+    return {"workload": "HEA %d qubits, %d layers, %d parameters, periodic XXZ (%d terms)" % (n, layers, theta.size,
+                                                                                             len(terms)),
+            "grad_per_s_fp32": 1.0 / t_adj, "seconds_per_grad_fp32": t_adj, "energy_fp32": e32, "energy_fp64": e64,
+            "rel_err_fp32_vs_fp64_adjoint": rel32, "rel_err_fp64_adjoint_vs_fd_subset": rel_fd,
+            "rel_err_fp32_adjoint_vs_fd_subset": rel_fd32, "fd_subset": [int(x) for x in ids]}
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -188,10 +238,30 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+def profile_case_fused26():
+    """Small case for ncu (26 qubits FP32 = 512 MB, larger than L2): the first 8 ops of the
+    fused k<=6 plan of the 26-qubit random circuit, twice (k_fused_tc and k_diagk launches)."""
+    import __graft_entry__ as ge
+    qi = ge.load_package()
+    from quant_iron_gb300 import workloads
+    n = 26
+    gates = workloads.random_circuit(n, LAYERS, seed=SEED)
+    plan = qi.Plan(n, qi.F32, gates, fusion=qi.FUSION_GREEDY, max_block_qubits=FUSED_K)
+    st = qi.DeviceState(n, qi.F32)
+    st.set_plus()
+    for _ in range(2):
+        plan.execute(st)
+    st.synchronize()
+    print("profile case done, norm^2 = %.9f" % st.norm_sqr())
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+        return
+    if args.profile_case == "fused26":
+        profile_case_fused26()
         return
     import numpy as np
     import torch
@@ -269,8 +339,16 @@ def main():
     pass_bytes = (1 << n) * 8 * 2   # one read + one write of every FP32 amplitude
     avg_ms = by_kernel[dom]["ms"] / by_kernel[dom]["launches"]
     achieved = pass_bytes / (avg_ms / 1e3) / 1e9
+    # DRAM traffic per launch from the committed ncu capture of a smaller case of the same kernel,
+    # scaled by amplitude count (traffic grows in proportion to the state)
+    traffic, traffic_src = None, None
+    prof = os.path.join(ROOT, "profiles", "k_fused_tc_fused26_ncu.json")
+    if dom == "k_fused_tc" and os.path.exists(prof):
+        pj = json.load(open(prof))
+        traffic = pj["traffic_per_amp_bytes"] * (1 << n)
+        traffic_src = "profiles/k_fused_tc_fused26.md (26-qubit capture x 2^%d)" % (n - 26)
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": None, "kernel": dom, "peak_source": peak_kind,
+                "traffic": traffic, "traffic_source": traffic_src, "kernel": dom, "peak_source": peak_kind,
                 "algorithmic_bytes_per_launch": pass_bytes, "avg_launch_ms": avg_ms,
                 "kernels": {k: {"launches": v["launches"], "ms": round(v["ms"], 3),
                                 "share": round(v["ms"] / max(1e-9, sum(x["ms"] for x in by_kernel.values())), 4)}
@@ -323,6 +401,7 @@ def main():
                  "energy_fused_fp32": energy, "energy_fp64_per_gate": energy64,
                  "energy_error": abs(energy - energy64),
                  "gates_per_s_fused": len(gates) / (ms_per_step / 1e3)}
+        extra["adjoint"] = adjoint_leg(qi, workloads, stream, torch, np)
 
     # end-to-end through the public API with host buffers: H2D of the initial state,
     # the circuit, D2H of the final state, every step

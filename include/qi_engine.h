@@ -310,6 +310,33 @@ qi_status qi_adjoint_gradient(qi_state *s, const qi_gate *gates, int64_t n_gates
                               const qi_exec_options *forward_opts, double *energy_out, double *grads_out);
 
 /* ------------------------------------------------------------------------ */
+/* Measurement (src/components/state.rs:525-784, measurement.rs:15-101)       */
+/* ------------------------------------------------------------------------ */
+#define QI_BASIS_COMPUTATIONAL 0   /* MeasurementBasis::Computational */
+#define QI_BASIS_X             1   /* H before and after (state.rs:671-690) */
+#define QI_BASIS_Y             2   /* S-dagger then H before, H then S after (state.rs:691-712) */
+#define QI_BASIS_CUSTOM        3   /* U before, U-dagger after (state.rs:713-729) */
+/* `State::measure`: outcome probabilities of the measured qubits (bit k of the
+ * outcome integer = qubit qubits[k]; n_qubits == 0 measures all qubits in
+ * order) summed in FP64 on the device, normalised, one uniform draw
+ * r = (splitmix64(seed) >> 11) * 2^-53 (the reference draws from an unseeded
+ * rand::rng(), state.rs:601), CDF scan `r < cumulative` in outcome order,
+ * collapse and renormalisation in place.  custom_u (8 doubles, Unitary2
+ * layout) only for QI_BASIS_CUSTOM.  probs_out (2^m doubles, may be NULL)
+ * receives the normalised probabilities.  Errors: InvalidNumberOfQubits when
+ * more qubits than the state has, InvalidQubitIndex(q, n), UnknownError when
+ * the total probability is below f64::EPSILON (state.rs:593-595).
+ * Measuring more than 24 qubits returns Unsupported. */
+qi_status qi_measure(qi_state *s, int32_t basis, const double *custom_u, const int32_t *qubits, int32_t n_qubits,
+                     uint64_t seed, uint64_t *outcome_out, double *probs_out);
+/* `State::measure_n` (state.rs:750-784): n_shots outcomes drawn from the same
+ * pre-measurement distribution (shot j uses splitmix64(seed + j)); the state
+ * is left unchanged (the basis change is undone).  InvalidNumberOfMeasurements(0)
+ * for n_shots == 0. */
+qi_status qi_measure_n(qi_state *s, int32_t basis, const double *custom_u, const int32_t *qubits, int32_t n_qubits,
+                       int64_t n_shots, uint64_t seed, uint64_t *outcomes_out);
+
+/* ------------------------------------------------------------------------ */
 /* Learned fusion cost model (no reference counterpart)                      */
 /* ------------------------------------------------------------------------ */
 /* An MLP (20 features -> 3 x 64 ReLU -> 1) predicting y = log(device ms per

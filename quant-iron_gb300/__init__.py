@@ -315,6 +315,51 @@ def apply_matrix(state, targets, matrix, use_tensor_cores=0):
                               int(use_tensor_cores)))
 
 
+def _basis_args(basis, custom):
+    b = _abi.BASIS[basis] if isinstance(basis, str) else int(basis)
+    u = None
+    if custom is not None:
+        m = np.asarray(custom, dtype=np.complex128).reshape(2, 2)
+        u = np.array([m[0, 0].real, m[0, 0].imag, m[0, 1].real, m[0, 1].imag, m[1, 0].real, m[1, 0].imag,
+                      m[1, 1].real, m[1, 1].imag])
+    return b, u
+
+
+def splitmix_uniform(seed):
+    """The uniform draw qi_measure uses for `seed`: (splitmix64(seed) >> 11) * 2^-53."""
+    m = (1 << 64) - 1
+    x = (seed + 0x9E3779B97F4A7C15) & m
+    x = ((x ^ (x >> 30)) * 0xBF58476D1CE4E5B9) & m
+    x = ((x ^ (x >> 27)) * 0x94D049BB133111EB) & m
+    x ^= x >> 31
+    return (x >> 11) * 2.0 ** -53
+
+
+def measure(state, qubits=(), basis="Computational", custom=None, seed=0, return_probs=False):
+    """State::measure on the device (state collapses in place); returns the outcome integer
+    (bit k = qubit qubits[k]) and optionally the normalised probabilities."""
+    b, u = _basis_args(basis, custom)
+    q = np.ascontiguousarray(qubits, dtype=np.int32)
+    m = q.size if q.size else state.n
+    out = ctypes.c_uint64()
+    probs = np.zeros(1 << m, dtype=np.float64) if return_probs else None
+    pd = ctypes.POINTER(ctypes.c_double)
+    check(lib.qi_measure(state.h, b, u.ctypes.data_as(pd) if u is not None else None, q.ctypes.data if q.size else None,
+                         q.size, int(seed), ctypes.byref(out), probs.ctypes.data_as(pd) if probs is not None else None))
+    return (out.value, probs) if return_probs else out.value
+
+
+def measure_n(state, n_shots, qubits=(), basis="Computational", custom=None, seed=0):
+    """State::measure_n: n_shots outcomes of the same distribution; the state is unchanged."""
+    b, u = _basis_args(basis, custom)
+    q = np.ascontiguousarray(qubits, dtype=np.int32)
+    out = np.zeros(max(int(n_shots), 1), dtype=np.uint64)
+    pd = ctypes.POINTER(ctypes.c_double)
+    check(lib.qi_measure_n(state.h, b, u.ctypes.data_as(pd) if u is not None else None, q.ctypes.data if q.size else None,
+                           q.size, int(n_shots), int(seed), out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64))))
+    return out[:n_shots]
+
+
 def adjoint_gradient(state, gates, theta, terms, fusion=FUSION_GREEDY, max_block_qubits=0, use_tensor_cores=0):
     """dE/dtheta of E = <psi(theta)|H|psi(theta)> by one forward and one reverse sweep.
     `state` holds |psi0> before and after the call.  Returns (E, grads)."""

@@ -191,6 +191,11 @@ for _name, _args in {
     getattr(lib, _name).restype = _i32
     getattr(lib, _name).argtypes = _args
 COSTMODEL_FEATURES = 20
+lib.qi_measure.restype = _i32
+lib.qi_measure.argtypes = [_vp, _i32, _pd, _vp, _i32, _u64, ctypes.POINTER(_u64), _pd]
+lib.qi_measure_n.restype = _i32
+lib.qi_measure_n.argtypes = [_vp, _i32, _pd, _vp, _i32, _i64, _u64, ctypes.POINTER(_u64)]
+BASIS = {"Computational": 0, "X": 1, "Y": 2, "Custom": 3}
 lib.qi_sumop_expectation_noalloc.restype = _i32
 lib.qi_sumop_expectation_noalloc.argtypes = [_vp, _i32, _i32, _vp, _i64, _vp, _pd]
 lib.qi_adjoint_gradient.restype = _i32

@@ -4,24 +4,40 @@
 //
 // For a tile of 128 columns (the 7 lowest non-target qubits, plus the tile's
 // fixed high bits) the block computes OUT[n][m] = sum_r U[n][r] X[r][m] with
-// R = 2^k rows.  As a real GEMM with M = 128 (tile columns) and K = 2R:
-//   A[m][k]   = Re X[k][m] (k < R), Im X[k-R][m] (k >= R)      — tensor memory
-//   D_re[m][n] = sum_{k<R} A[m][k] Re U[n][k] + A[m][R+k] (-Im U[n][k])
-//   D_im[m][n] = sum_{k<R} A[m][k] Im U[n][k] + A[m][R+k] ( Re U[n][k])
-// so the B operands are the R x R blocks Re U, Im U and -Im U (K-major,
-// shared memory), each N = R wide.  Every operand is split as x = hi + lo
-// with hi = tf32(x) (round to nearest) and lo = tf32(x - hi); the products
+// R = 2^k rows.  As a real GEMM with M = 128 (tile columns), N = 2R and the
+// K dimension split into a real half and an imaginary half of R each:
+//   [D_re | D_im][m] += Re X[.][m] . [ Re U ; Im U ]^T     (real half)
+//   [D_re | D_im][m] += Im X[.][m] . [-Im U ; Re U ]^T     (imaginary half)
+// The B operands are the R x R blocks -Im U, Re U, Im U stored one after the
+// other along N (K-major, shared memory), so [Re U ; Im U] starts at block 1
+// and [-Im U ; Re U] at block 0.  Every operand is split as x = hi + lo with
+// hi = tf32(x) (round to nearest) and lo = tf32(x - hi); the products
 // A_hi B_hi + A_hi B_lo + A_lo B_hi are accumulated in FP32, which keeps
 // about 22 significant bits (the dropped A_lo B_lo term is ~2^-22 relative).
 //
-// Per tile (one CTA of 16 warps per SM, persistent):
-//   16 warps read the tile (qi_tile.cuh, [row][column] layout), split hi/lo
-//   and tcgen05.st A_hi / A_lo to TMEM (warp w: lanes 32*(w%4).., rows slice w/4)
-//   one thread issues the 6 * 2R/8 MMAs (M128 x N=R x K8) and commits to an
-//   mbarrier; every wait on it is bounded and a timeout sets the error flag
-//   while the MMAs run: store tile t-1's output, cp.async-prefetch tile t+1
-//   16 warps tcgen05.ld D and write OUT into the tile buffer.
-// Tensor-memory columns: A_hi [0, 2R), A_lo [2R, 4R), D_re [4R, 5R), D_im [5R, 6R).
+// One persistent CTA per SM, warp-specialised, synchronised by mbarriers:
+//   producer (1 thread): cp.async.bulk copies of each tile (2^nhigh runs of
+//     2^L contiguous amplitudes) into one of NBUF shared buffers, in address
+//     order; completion by transaction count on raw_full[b]
+//   converters (8 warps; warp w owns TMEM lanes 32*(w%4).. = tile columns and
+//     rows slice w/4): once A stage 0 is free, read the tile in 16-row chunks,
+//     splitting the real parts into A_hi/A_lo of stage 0 (tcgen05.st) and
+//     keeping the imaginary parts in registers; release the buffer
+//     (raw_empty[b]); split the imaginary parts into stage 1 once it is free;
+//     each stage is signalled on a_full[h]
+//   MMA issuer (1 thread): per half 3 products x R/8 MMAs (M128 x N2R x K8)
+//     into accumulator buffer it%2; tcgen05.commit frees the A stage
+//     (a_empty[h]) and publishes the accumulator (d_full[d])
+//   epilogue (4 warps): tcgen05.ld the accumulator, release it (d_empty[d]),
+//     store the amplitudes straight to global memory (rows r, r+1 as one
+//     16-byte store when qubit 0 is a target; adjacent lanes are adjacent
+//     amplitudes when it is a column)
+// Every wait is bounded; a timeout sets the state's error flag (2) and a
+// shared abort flag that every other wait polls, so all roles leave their
+// loops; the MMA thread then waits for its own products and the producer for
+// its copies before the tensor memory is freed.
+// Tensor-memory columns: A stage h at h*2R (A_hi [0,R), A_lo [R,2R)),
+// accumulator d at 4R + d*2R (D_re [0,R), D_im [R,2R)): 8R columns in all.
 #include "qi_internal.hpp"
 #include "qi_device.cuh"
 #include "qi_tile.cuh"
@@ -31,7 +47,9 @@
 
 namespace qi {
 
-constexpr int kTcThreads = 512;   // 16 warps: 4 lane quarters x 4 row slices
+constexpr int kConvWarps = 8, kEpiWarps = 4;
+constexpr int kProducerWarp = kConvWarps + kEpiWarps, kMmaWarp = kProducerWarp + 1;
+constexpr int kTcThreads = (kMmaWarp + 1) * 32;   // 448
 constexpr uint32_t kWaitLimit = 1u << 22;   // bounded mbarrier wait (iterations of try_wait)
 
 // ---------------------------------------------------------- PTX wrappers --
@@ -175,49 +193,148 @@ __device__ __forceinline__ void tmem_ld<32>(uint32_t taddr, uint32_t (&v)[32]) {
 __device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;\n" ::: "memory"); }
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory"); }
 
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(smem_u32(bar)) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+// Contiguous global -> shared copy on the bulk-copy engine; completes `bytes`
+// of the barrier's transaction count.  Both addresses 16-byte aligned, bytes % 16 == 0.
+__device__ __forceinline__ void bulk_load(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
+                     smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+
+// Bounded wait that also gives up when another role raised the abort flag;
+// a timeout raises it and records status 2 in the state's error flag.
+__device__ __forceinline__ bool wait_or_abort(uint64_t *bar, uint32_t parity, volatile int *abort_flag, int *err_flag) {
+    for (uint32_t i = 0; i < kWaitLimit; ++i) {
+        if (mbar_try_wait(bar, parity)) return true;
+        if ((i & 31u) == 31u && *abort_flag) return false;
+    }
+    *abort_flag = 1;
+    atomicExch(err_flag, 2);   // 2 = a bounded device wait ran out (1 is ZeroNorm)
+    return false;
+}
+// Warp-uniform form: every lane waits, the warp proceeds only if all saw the phase.
+__device__ __forceinline__ bool warp_wait_or_abort(uint64_t *bar, uint32_t parity, volatile int *abort_flag,
+                                                   int *err_flag) {
+    const bool ok = wait_or_abort(bar, parity, abort_flag, err_flag);
+    return __all_sync(0xffffffffu, ok);
+}
+
 // ------------------------------------------------------------------ kernel
 template <int K>
 struct TcCfg {
-    static constexpr int R = 1 << K;            // rows (target patterns)
-    static constexpr int KR = 2 * R;            // real K of the GEMM
-    static constexpr int H = R / 4;             // rows per warp slice
-    static constexpr int BLK = R * R;           // floats per operand block
-    static constexpr uint32_t LBO = 128;        // next core matrix along K
-    static constexpr uint32_t SBO = (R / 4) * 128;   // next 8-row group along N
-    static constexpr uint32_t TMEM_COLS = K == 6 ? 512 : 256;
-    static constexpr uint32_t COL_AHI = 0, COL_ALO = KR, COL_D = 2 * KR;
-    static constexpr size_t SMEM_B = 6 * BLK * sizeof(float);
-    static constexpr size_t SMEM_TILE = (size_t)R * 128 * sizeof(float2);
-    static constexpr size_t SMEM = SMEM_B + 2 * SMEM_TILE + 32 * sizeof(TileIterTab) + 64;
+    static constexpr int R = 1 << K;                   // rows (target patterns)
+    static constexpr int BLK = R * R;                  // floats per operand block
+    static constexpr uint32_t LBO = 128;               // next core matrix along K
+    static constexpr uint32_t SBO = (R / 4) * 128;     // next 8-row group along N
+    static constexpr int NBUF = K == 6 ? 2 : 4;        // tile buffers in shared memory
+    static constexpr uint32_t STAGE = 2 * R;           // TMEM columns of one A stage or one accumulator
+    static constexpr uint32_t COL_A = 0, COL_D = 2 * STAGE;
+    static constexpr uint32_t TMEM_COLS = 4 * STAGE;   // 512 for k = 6, 256 for k = 5
+    static constexpr int CONV_ROWS = R / 2;            // rows per converter thread (2 row slices)
+    static constexpr int CHUNK = 16;                   // rows converted per step (register footprint)
+    static constexpr uint32_t TILE_BYTES = (uint32_t)R * 128 * sizeof(float2);
+    static constexpr size_t OFF_TILES = 6 * (size_t)BLK * sizeof(float);
+    static constexpr size_t OFF_ROWX = OFF_TILES + (size_t)NBUF * TILE_BYTES;
+    static constexpr size_t OFF_GROW = OFF_ROWX + 64 * sizeof(uint32_t);
+    static constexpr size_t OFF_BAR = OFF_GROW + 64 * sizeof(uint64_t);
+    static constexpr int NBARS = 2 * NBUF + 9;
+    static constexpr size_t OFF_MISC = OFF_BAR + NBARS * sizeof(uint64_t);
+    static constexpr size_t SMEM = OFF_MISC + 16;
 };
+
+// Tile-local position of column m: its bits deposited, in order, on the bits
+// below L that are not targets.
+__device__ __forceinline__ uint32_t tile_colx(const TileGeom &g, uint32_t m) {
+    uint32_t x = 0;
+    int j = 0;
+    for (int q = 0; q < g.L; ++q) {
+        bool tgt = false;
+        for (int u = 0; u < g.nlow_t; ++u) tgt |= (g.low_t[u] == q);
+        if (!tgt) {
+            x |= ((m >> j) & 1u) << q;
+            ++j;
+        }
+    }
+    return x;
+}
+
+// x = hi + lo split of N rows of one column into A_hi / A_lo tensor-memory columns.
+// x is left holding x - hi.
+template <int N>
+__device__ __forceinline__ void split_store(uint32_t taddr_hi, uint32_t taddr_lo, float (&x)[N]) {
+    uint32_t v[N];
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+        v[i] = tf32_rna(x[i]);
+        x[i] -= __uint_as_float(v[i]);
+    }
+    tmem_st<N>(taddr_hi, v);
+#pragma unroll
+    for (int i = 0; i < N; ++i) v[i] = tf32_rna(x[i]);
+    tmem_st<N>(taddr_lo, v);
+}
 
 template <int K>
 __global__ void __launch_bounds__(kTcThreads, 1) k_fused_tc(float2 *a, const float *blocks, TileGeom g, int *err_flag) {
     using C = TcCfg<K>;
-    constexpr int R = C::R, H = C::H;
+    constexpr int R = C::R, NB = C::NBUF;
     extern __shared__ __align__(1024) unsigned char smem_raw[];
-    float *sB = reinterpret_cast<float *>(smem_raw);                      // 6 operand blocks
-    float2 *S0 = reinterpret_cast<float2 *>(smem_raw + C::SMEM_B);
-    float2 *S1 = S0 + R * 128;
-    TileIterTab *tab = reinterpret_cast<TileIterTab *>(S1 + R * 128);
-    uint64_t *mbar = reinterpret_cast<uint64_t *>(tab + 32);
-    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(mbar + 1);
+    float *sB = reinterpret_cast<float *>(smem_raw);   // 6 operand blocks: -Im, Re, Im (hi), then (lo)
+    unsigned char *tiles = smem_raw + C::OFF_TILES;
+    uint32_t *rowx = reinterpret_cast<uint32_t *>(smem_raw + C::OFF_ROWX);
+    uint64_t *grow = reinterpret_cast<uint64_t *>(smem_raw + C::OFF_GROW);
+    uint64_t *raw_full = reinterpret_cast<uint64_t *>(smem_raw + C::OFF_BAR);
+    uint64_t *raw_empty = raw_full + NB, *a_full = raw_empty + NB, *a_empty = a_full + 2;
+    uint64_t *d_full = a_empty + 2, *d_empty = d_full + 2, *mma_done = d_empty + 2;
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(smem_raw + C::OFF_MISC);
     volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int quarter = warp & 3, half = warp >> 2;   // lane quarter, row slice (0..3)
 
     // operand blocks -> shared memory (16-byte vectors), visible to the async proxy
     {
         const uint4 *src = reinterpret_cast<const uint4 *>(blocks);
         uint4 *dst = reinterpret_cast<uint4 *>(sB);
-        for (int i = tid; i < (int)(C::SMEM_B / 16); i += kTcThreads) dst[i] = src[i];
+        for (int i = tid; i < (int)(C::OFF_TILES / 16); i += kTcThreads) dst[i] = src[i];
     }
     asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-    const TileWalk w = tile_walk_init(g, tid, kTcThreads);
-    if (tid < w.iters) tile_iter_fill(g, kTcThreads, tid, tab);
+    // row r (bit j <-> target j) -> tile-local position and global offset
+    if (tid < R) {
+        uint32_t x = 0;
+        uint64_t go = 0;
+        for (int j = 0; j < g.nlow_t; ++j) {
+            const uint32_t bit = ((uint32_t)tid >> j) & 1u;
+            x |= bit << g.low_t[j];
+            go |= (uint64_t)bit << g.low_t[j];
+        }
+        for (int j = 0; j < g.nhigh; ++j) {
+            const uint32_t bit = ((uint32_t)tid >> (g.nlow_t + j)) & 1u;
+            x |= bit << (g.L + j);
+            go |= (uint64_t)bit << g.high_t[j];
+        }
+        rowx[tid] = x;
+        grow[tid] = go;
+    }
     if (tid == 0) {
-        mbar_init(mbar, 1);
+        for (int i = 0; i < NB; ++i) {
+            mbar_init(raw_full + i, 1);
+            mbar_init(raw_empty + i, kConvWarps);
+        }
+        for (int i = 0; i < 2; ++i) {
+            mbar_init(a_full + i, kConvWarps);
+            mbar_init(a_empty + i, 1);
+            mbar_init(d_full + i, 1);
+            mbar_init(d_empty + i, kEpiWarps);
+        }
+        mbar_init(mma_done, 1);
         *abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
     }
@@ -226,116 +343,168 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_fused_tc(float2 *a, const flo
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = *tmem_slot;
-    const uint32_t lane_base = (uint32_t)(quarter * 32) << 16;
-    const int m = quarter * 32 + lane;   // this thread's tile column / TMEM lane
+    const uint64_t ntiles = g.ntiles, t0 = blockIdx.x, tstep = gridDim.x;
+    const bool pair_rows = !g.q0_is_col;   // qubit 0 is target 0: rows r, r+1 are adjacent amplitudes
 
-    // Descriptor of block 0 at K offset 0; every MMA adds a constant byte offset
-    // (>> 4 into the start-address field, which cannot carry: blocks stay below 256 KB).
-    const uint64_t desc0 = smem_desc(smem_u32(sB), C::LBO, C::SBO);
-    const uint32_t idesc = tf32_idesc(128, R);
-
-    // Software pipeline over this CTA's tiles (buffers alternate):
-    //   wait tile t -> convert(t) -> issue MMA(t) -> store output of tile t-1 and
-    //   prefetch tile t+1 into its buffer while the MMAs run -> wait -> epilogue(t)
-    uint64_t t = blockIdx.x;
-    if (t < g.ntiles) tile_load_async(g, w, tab, a, tile_base(g, t), S0);
-    cp_async_commit();
-
-    uint64_t prev_t = 0;
-    int it = 0;
-    for (; t < g.ntiles; ++it, t += gridDim.x) {
-        float2 *S = (it & 1) ? S1 : S0;
-        float2 *Sprev = (it & 1) ? S0 : S1;
-        cp_async_wait<0>();
-        __syncthreads();
-        if (*abort_flag) break;
-
-        // ---- convert: rows [half*H, half*H + H) of column m -> A_hi / A_lo
-        {
-            const int r0 = half * H;
-            uint32_t hi_re[H], hi_im[H];
-            float lo_re[H], lo_im[H];
-#pragma unroll
-            for (int i = 0; i < H; ++i) {
-                const float2 x = S[tile_sidx(g, r0 + i, m)];
-                hi_re[i] = tf32_rna(x.x);
-                hi_im[i] = tf32_rna(x.y);
-                lo_re[i] = x.x - __uint_as_float(hi_re[i]);
-                lo_im[i] = x.y - __uint_as_float(hi_im[i]);
-            }
-            tmem_st<H>(tmem + lane_base + C::COL_AHI + r0, hi_re);
-            tmem_st<H>(tmem + lane_base + C::COL_AHI + R + r0, hi_im);
-            uint32_t lr[H], li[H];
-#pragma unroll
-            for (int i = 0; i < H; ++i) {
-                lr[i] = tf32_rna(lo_re[i]);
-                li[i] = tf32_rna(lo_im[i]);
-            }
-            tmem_st<H>(tmem + lane_base + C::COL_ALO + r0, lr);
-            tmem_st<H>(tmem + lane_base + C::COL_ALO + R + r0, li);
-            tmem_wait_st();
-        }
-        tc_fence_before();
-        __syncthreads();
-
-        // ---- MMA: one thread issues all products, commits to the mbarrier
-        if (tid == 0) {
+    if (warp < kConvWarps) {
+        // ------------------------------------------------ converters
+        const int quarter = warp & 3, slice = warp >> 2;
+        const uint32_t cx = tile_colx(g, (uint32_t)(quarter * 32 + lane));
+        const uint32_t lane_base = (uint32_t)(quarter * 32) << 16;
+        const int r0 = slice * C::CONV_ROWS;
+        int it = 0;
+        for (uint64_t t = t0; t < ntiles; t += tstep, ++it) {
+            const int b = it % NB;
+            if (!warp_wait_or_abort(raw_full + b, (uint32_t)(it / NB) & 1u, abort_flag, err_flag)) break;
+            const float2 *S = reinterpret_cast<const float2 *>(tiles + (size_t)b * C::TILE_BYTES);
+            // real half -> A stage 0, once the products of the previous tile have read it;
+            // the imaginary parts stay in registers for stage 1
+            if (it > 0 && !warp_wait_or_abort(a_empty + 0, (uint32_t)(it - 1) & 1u, abort_flag, err_flag)) break;
             tc_fence_after();
-            // block order in shared memory: 0 Re hi, 1 Im hi, 2 -Im hi, 3 Re lo, 4 Im lo, 5 -Im lo
+            float im[C::CONV_ROWS];
 #pragma unroll
-            for (int part = 0; part < 2; ++part) {
-                const uint32_t d = tmem + C::COL_D + part * R;
+            for (int c0 = 0; c0 < C::CONV_ROWS; c0 += C::CHUNK) {
+                float re[C::CHUNK];
+                if (pair_rows) {
 #pragma unroll
-                for (int prod = 0; prod < 3; ++prod) {
-                    const uint32_t acol = (prod == 2) ? C::COL_ALO : C::COL_AHI;   // A_hi, A_hi, A_lo
-                    const int bset = (prod == 1) ? 3 : 0;                          // B_hi, B_lo, B_hi
+                    for (int i = 0; i < C::CHUNK; i += 2) {
+                        const float4 v = *reinterpret_cast<const float4 *>(S + (rowx[r0 + c0 + i] | cx));
+                        re[i] = v.x;
+                        im[c0 + i] = v.y;
+                        re[i + 1] = v.z;
+                        im[c0 + i + 1] = v.w;
+                    }
+                } else {
 #pragma unroll
-                    for (int j = 0; j < C::KR / 8; ++j) {
-                        const int kk = 8 * j;
-                        const bool first_half = kk < R;
-                        const int blk = part == 0 ? (first_half ? 0 : 2) : (first_half ? 1 : 0);
-                        const int koff = first_half ? kk : kk - R;
-                        const uint32_t boff = (uint32_t)((bset + blk) * C::BLK * 4) + (uint32_t)(koff / 4) * C::LBO;
-                        mma_tf32_ts(d, tmem + acol + kk, desc0 + (uint64_t)(boff >> 4), idesc,
-                                    (prod == 0 && j == 0) ? 0u : 1u);
+                    for (int i = 0; i < C::CHUNK; ++i) {
+                        const float2 v = S[rowx[r0 + c0 + i] | cx];
+                        re[i] = v.x;
+                        im[c0 + i] = v.y;
                     }
                 }
+                split_store<C::CHUNK>(tmem + lane_base + C::COL_A + r0 + c0, tmem + lane_base + C::COL_A + R + r0 + c0,
+                                      re);
             }
-            mma_commit(mbar);
-        }
-        // ---- while the tensor cores run: store tile t-1's output, prefetch tile t+1
-        if (it > 0) tile_store(g, w, tab, a, tile_base(g, prev_t), Sprev);
-        __syncthreads();
-        const uint64_t nt = t + gridDim.x;
-        if (nt < g.ntiles) tile_load_async(g, w, tab, a, tile_base(g, nt), Sprev);
-        cp_async_commit();
-        // ---- wait for the products (bounded)
-        if (!mbar_wait_bounded(mbar, (uint32_t)(it & 1))) {
-            *abort_flag = 1;
-            atomicExch(err_flag, 2);   // 2 = a bounded device wait ran out (1 is ZeroNorm)
-        }
-        tc_fence_after();
-        __syncthreads();
-        if (*abort_flag) break;
-
-        // ---- epilogue: D rows [half*H, +H) of column m -> tile buffer
-        {
-            const int n0 = half * H;
-            uint32_t dr[H], di[H];
-            tmem_ld<H>(tmem + lane_base + C::COL_D + n0, dr);
-            tmem_ld<H>(tmem + lane_base + C::COL_D + R + n0, di);
-            tmem_wait_ld();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(raw_empty + b);   // the buffer may take the next tile
+            tmem_wait_st();
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(a_full + 0);
+            // imaginary half -> A stage 1
+            if (it > 0 && !warp_wait_or_abort(a_empty + 1, (uint32_t)(it - 1) & 1u, abort_flag, err_flag)) break;
+            tc_fence_after();
 #pragma unroll
-            for (int i = 0; i < H; ++i)
-                S[tile_sidx(g, n0 + i, m)] = make_float2(__uint_as_float(dr[i]), __uint_as_float(di[i]));
+            for (int c0 = 0; c0 < C::CONV_ROWS; c0 += C::CHUNK)
+                split_store<C::CHUNK>(tmem + lane_base + C::COL_A + C::STAGE + r0 + c0,
+                                      tmem + lane_base + C::COL_A + C::STAGE + R + r0 + c0,
+                                      *reinterpret_cast<float(*)[C::CHUNK]>(im + c0));
+            tmem_wait_st();
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(a_full + 1);
         }
-        tc_fence_before();
-        prev_t = t;
+    } else if (warp < kConvWarps + kEpiWarps) {
+        // ------------------------------------------------ epilogue
+        const int quarter = warp & 3;
+        const uint64_t cx = tile_colx(g, (uint32_t)(quarter * 32 + lane));
+        const uint32_t lane_base = (uint32_t)(quarter * 32) << 16;
+        int it = 0;
+        for (uint64_t t = t0; t < ntiles; t += tstep, ++it) {
+            const int d = it & 1;
+            if (!warp_wait_or_abort(d_full + d, (uint32_t)(it >> 1) & 1u, abort_flag, err_flag)) break;
+            tc_fence_after();
+            float2 *out = a + (tile_base(g, t) | cx);   // column base; rows add disjoint bits
+            const uint32_t dcol = tmem + lane_base + C::COL_D + d * C::STAGE;
+#pragma unroll
+            for (int c = 0; c < R / 16; ++c) {
+                uint32_t vr[16], vi[16];
+                tmem_ld<16>(dcol + 16 * c, vr);
+                tmem_ld<16>(dcol + R + 16 * c, vi);
+                tmem_wait_ld();
+                if (c == R / 16 - 1) {   // accumulator read out: the next tile but one may use it
+                    tc_fence_before();
+                    __syncwarp();
+                    if (lane == 0) mbar_arrive(d_empty + d);
+                }
+                if (pair_rows) {
+#pragma unroll
+                    for (int i = 0; i < 16; i += 2)
+                        __stcs(reinterpret_cast<float4 *>(out + grow[16 * c + i]),
+                               make_float4(__uint_as_float(vr[i]), __uint_as_float(vi[i]), __uint_as_float(vr[i + 1]),
+                                           __uint_as_float(vi[i + 1])));
+                } else {
+#pragma unroll
+                    for (int i = 0; i < 16; ++i)
+                        __stcs(out + grow[16 * c + i], make_float2(__uint_as_float(vr[i]), __uint_as_float(vi[i])));
+                }
+            }
+        }
+    } else if (warp == kProducerWarp) {
+        // ------------------------------------------------ producer (one thread)
+        if (lane == 0) {
+            const uint32_t run_bytes = (uint32_t)sizeof(float2) << g.L;
+            const int nruns = 1 << g.nhigh;
+            int it = 0, issued = 0;
+            for (uint64_t t = t0; t < ntiles; t += tstep, ++it) {
+                const int b = it % NB;
+                if (it >= NB && !wait_or_abort(raw_empty + b, (uint32_t)(it / NB - 1) & 1u, abort_flag, err_flag))
+                    break;
+                mbar_arrive_expect_tx(raw_full + b, C::TILE_BYTES);
+                const uint64_t base = tile_base(g, t);
+                unsigned char *dst = tiles + (size_t)b * C::TILE_BYTES;
+                for (int h = 0; h < nruns; ++h)
+                    bulk_load(dst + (size_t)h * run_bytes, a + (base | grow[h << g.nlow_t]), run_bytes, raw_full + b);
+                issued = it + 1;
+            }
+            // copies still in flight (only after an abort) land before the CTA exits
+            for (int j = issued > NB ? issued - NB : 0; j < issued; ++j)
+                if (!mbar_wait_bounded(raw_full + (j % NB), (uint32_t)(j / NB) & 1u)) atomicExch(err_flag, 2);
+        }
+        __syncwarp();
+    } else {
+        // ------------------------------------------------ MMA issuer (one thread)
+        if (lane == 0) {
+            // Descriptor of block 0 at K offset 0; every MMA adds a constant byte offset
+            // (>> 4 into the start-address field, which cannot carry: blocks stay below 256 KB).
+            const uint64_t desc0 = smem_desc(smem_u32(sB), C::LBO, C::SBO);
+            constexpr uint32_t idesc = tf32_idesc(128, 2 * R);
+            int it = 0;
+            bool ok = true;
+            for (uint64_t t = t0; ok && t < ntiles; t += tstep, ++it) {
+                const int d = it & 1;
+                if (it >= 2 && !wait_or_abort(d_empty + d, (uint32_t)((it >> 1) - 1) & 1u, abort_flag, err_flag))
+                    break;
+                tc_fence_after();
+                const uint32_t dcol = tmem + C::COL_D + d * C::STAGE;
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    if (!wait_or_abort(a_full + h, (uint32_t)it & 1u, abort_flag, err_flag)) {
+                        ok = false;
+                        break;
+                    }
+                    tc_fence_after();
+                    const uint32_t acol = tmem + C::COL_A + h * C::STAGE;
+#pragma unroll
+                    for (int p = 0; p < 3; ++p) {   // (A_hi, B_hi), (A_hi, B_lo), (A_lo, B_hi)
+                        const int blk = (p == 1 ? 3 : 0) + (h == 0 ? 1 : 0);
+#pragma unroll
+                        for (int j = 0; j < R / 8; ++j) {
+                            const uint32_t boff = (uint32_t)(blk * C::BLK * 4) + (uint32_t)(2 * j) * C::LBO;
+                            mma_tf32_ts(dcol, acol + (p == 2 ? R : 0) + 8 * j, desc0 + (uint64_t)(boff >> 4), idesc,
+                                        (h | p | j) ? 1u : 0u);
+                        }
+                    }
+                    mma_commit(a_empty + h);
+                }
+                if (ok) mma_commit(d_full + d);
+            }
+            // every product issued here has completed before the tensor memory is freed
+            mma_commit(mma_done);
+            if (!mbar_wait_bounded(mma_done, 0)) atomicExch(err_flag, 2);
+        }
+        __syncwarp();
     }
-    cp_async_wait<0>();
-    __syncthreads();
-    // output of the last tile (skipped if the loop stopped on a timeout)
-    if (it > 0 && !*abort_flag) tile_store(g, w, tab, a, tile_base(g, prev_t), ((it - 1) & 1) ? S1 : S0);
     tc_fence_before();
     __syncthreads();
     if (warp == 0) {
@@ -365,7 +534,7 @@ void tc_blocks(int k, const double *U, std::vector<float> &out) {
     for (int n = 0; n < R; ++n) {
         for (int kk = 0; kk < R; ++kk) {
             const double re = U[2 * ((size_t)n * R + kk)], im = U[2 * ((size_t)n * R + kk) + 1];
-            const double vals[3] = {re, im, -im};
+            const double vals[3] = {-im, re, im};   // block order along N: -Im U, Re U, Im U
             const size_t off = ((size_t)(n / 8) * sbo + (size_t)(kk / 4) * 128 + (size_t)(n % 8) * 16 + (kk % 4) * 4) / 4;
             for (int b = 0; b < 3; ++b) {
                 const float hi = tf32_round_host(vals[b]);
@@ -380,13 +549,18 @@ void tc_blocks(int k, const double *U, std::vector<float> &out) {
 template <int K>
 static Status launch_tc_t(qi_state *s, const TileGeom &g, const void *d_tc) {
     using C = TcCfg<K>;
+    static_assert(C::SMEM <= 232448, "shared memory per CTA");
     static bool attr_set = false;
+    static int num_sms = 0;
     if (!attr_set) {
         QI_CUDA(cudaFuncSetAttribute(k_fused_tc<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::SMEM));
+        int dev = 0;
+        QI_CUDA(cudaGetDevice(&dev));
+        QI_CUDA(cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, dev));
         attr_set = true;
     }
-    uint64_t grid = g.ntiles;
-    if (grid > 152) grid = 152;
+    uint64_t grid = g.ntiles;   // one persistent CTA per SM
+    if (grid > (uint64_t)num_sms) grid = (uint64_t)num_sms;
     k_fused_tc<K><<<(unsigned)grid, kTcThreads, C::SMEM, s->stream>>>((float2 *)s->amps, (const float *)d_tc, g,
                                                                       s->d_flag);
     count_launch();

@@ -57,6 +57,27 @@ def test_tensor_core_block_vs_numpy(qi, k, n):
 
 
 @pytest.mark.parametrize("k", [5, 6])
+def test_tensor_core_many_tiles_per_sm(qi, k):
+    """n = 23: 1024 (k = 6) or 2048 (k = 5) tiles, several per persistent CTA,
+    so every shared buffer, A stage and accumulator is reused and every
+    barrier goes through both phases."""
+    n = 23
+    sets = {6: [[0, 1, 2, 3, 4, 5], [0, 6, 9, 17, 21, 22], [2, 3, 10, 15, 20, 22]],
+            5: [[0, 1, 2, 3, 4], [0, 7, 16, 21, 22], [1, 5, 12, 19, 22]]}[k]
+    init = rand_state(n, 5)
+    for i, targets in enumerate(sets):
+        U = haar(k, 100 + i)
+        want = apply_np(init, n, targets, U)
+        with qi.DeviceState(n, qi.F32) as st:
+            st.upload(init)
+            qi.apply_matrix(st, targets, U, use_tensor_cores=1)
+            got = st.download()
+        err = np.max(np.abs(got - want))
+        infid = 1 - abs(np.vdot(want, got)) ** 2 / np.vdot(got, got).real
+        assert err < 1e-6 and infid < 1e-10, (k, targets, err, infid)
+
+
+@pytest.mark.parametrize("k", [5, 6])
 def test_tensor_core_matches_cuda_core_path(qi, k):
     n = 15
     targets = [1, 4, 5, 9, 12, 14][:k]

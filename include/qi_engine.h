@@ -366,18 +366,23 @@ qi_status qi_costmodel_set_params(const float *in, int64_t count, int32_t traine
  * Lets tests check the fusion pass without a GPU. */
 typedef struct qi_plan_op_info {
     int32_t  kind;          /* 1 one-target gate, 2 SWAP, 3 two-target gate, 4 fused dense block,
-                               5 Pauli exponential, 6 Pauli string + normalise, 7 diagonal block */
-    int32_t  k;             /* number of targets */
+                               5 Pauli exponential, 6 Pauli string + normalise, 7 diagonal block,
+                               8 renormalisation, 9 phase polynomial (a run of diagonal blocks) */
+    int32_t  k;             /* number of targets (kind 9: number of diagonal blocks in the run) */
     int32_t  targets[6];    /* sorted ascending for kinds 3, 4, 7 */
     int32_t  tensor_cores;  /* kind 4: 1 if the block runs on the tcgen05 tensor-core kernel */
     int32_t  reserved;
     uint64_t control_mask;
-    uint64_t xmask, zmask;  /* kinds 5 and 6 */
+    uint64_t xmask, zmask;  /* kinds 5 and 6; kind 9: zmask = the qubits the run touches */
     int64_t  n_matrix;      /* complex entries of the op's matrix: 4 (kind 1), 16 (kind 3), 4^k (kind 4),
                                2^k (kind 7: the diagonal), 2 (kind 5: cosh(alpha), sinh(alpha)), else 0 */
 } qi_plan_op_info;
 qi_status qi_plan_num_ops(const qi_plan *p, int64_t *out);
 qi_status qi_plan_op_get(const qi_plan *p, int64_t i, qi_plan_op_info *info, double *matrix_out, int64_t capacity);
+/* Kind 9 ops: the phase polynomial f(x) = c0 + sum_q a[q] x_q + sum_{q<r} b[q*n+r] x_q x_r
+ * applied as exp(2 pi i f / 2^64) (coefficients in units of 2^-64 turns; a: n entries,
+ * b: n*n entries, zero for q >= r).  Introspection aid; no reference counterpart. */
+qi_status qi_plan_op_phase_poly(const qi_plan *p, int64_t i, uint64_t *c0, uint64_t *a, uint64_t *b);
 /* Execute the plan once with a CUDA event pair around every operation, on the
  * state's stream, and write each operation's device time in milliseconds to
  * ms_out (qi_plan_num_ops entries).  Measurement aid; no reference counterpart. */

@@ -175,6 +175,7 @@ class Plan:
     def __init__(self, num_qubits, precision, gates, theta=None, fusion=FUSION_NONE, max_block_qubits=0,
                  use_tensor_cores=0, renorm_every=0):
         gates = np.ascontiguousarray(gates, dtype=GATE_DTYPE)
+        self.num_qubits = int(num_qubits)
         self.h = ctypes.c_void_p()
         opts = _options(fusion, max_block_qubits, use_tensor_cores, renorm_every)
         tp, tn, self._keep = _theta_arg(theta)
@@ -203,10 +204,19 @@ class Plan:
             check(lib.qi_plan_op_get(self.h, i, ctypes.byref(info), buf.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
                                      info.n_matrix))
             mat = buf[0::2][:info.n_matrix] + 1j * buf[1::2][:info.n_matrix]
-            out.append({"kind": info.kind, "k": info.k, "targets": list(info.targets)[:max(info.k, 0)],
-                        "tensor_cores": info.tensor_cores,
-                        "control_mask": info.control_mask, "xmask": info.xmask, "zmask": info.zmask,
-                        "matrix": mat})
+            op = {"kind": info.kind, "k": info.k, "targets": list(info.targets)[:max(info.k, 0)],
+                  "tensor_cores": info.tensor_cores,
+                  "control_mask": info.control_mask, "xmask": info.xmask, "zmask": info.zmask,
+                  "matrix": mat}
+            if info.kind == 9:   # phase polynomial: coefficients in units of 2^-64 turns
+                nq = self.num_qubits
+                c0 = ctypes.c_uint64()
+                a = np.zeros(nq, dtype=np.uint64)
+                b = np.zeros(nq * nq, dtype=np.uint64)
+                check(lib.qi_plan_op_phase_poly(self.h, i, ctypes.byref(c0), a.ctypes.data, b.ctypes.data))
+                op["targets"] = [q for q in range(nq) if (info.zmask >> q) & 1]
+                op["poly"] = (np.uint64(c0.value), a, b.reshape(nq, nq))
+            out.append(op)
         return out
 
     def close(self):
@@ -295,7 +305,7 @@ def trotter_evolve(state, terms, dt, num_steps, order=1, observable=None, observ
 
 
 KERNEL_OF_OP_KIND = {1: "k_mat1", 2: "k_swap", 3: "k_mat2", 4: "k_fused", 5: "k_pauli_exp", 6: "k_pauli_exp+normalise",
-                     7: "k_diagk", 8: "k_norm_partial+k_normalise_apply"}
+                     7: "k_diagk", 8: "k_norm_partial+k_normalise_apply", 9: "k_phase_poly"}
 
 
 def plan_profile(plan, state):

@@ -198,5 +198,7 @@ lib.qi_measure_n.argtypes = [_vp, _i32, _pd, _vp, _i32, _i64, _u64, ctypes.POINT
 BASIS = {"Computational": 0, "X": 1, "Y": 2, "Custom": 3}
 lib.qi_sumop_expectation_noalloc.restype = _i32
 lib.qi_sumop_expectation_noalloc.argtypes = [_vp, _i32, _i32, _vp, _i64, _vp, _pd]
+lib.qi_plan_op_phase_poly.restype = _i32
+lib.qi_plan_op_phase_poly.argtypes = [_vp, _i64, ctypes.POINTER(_u64), _vp, _vp]
 lib.qi_adjoint_gradient.restype = _i32
 lib.qi_adjoint_gradient.argtypes = [_vp, _vp, _i64, _pd, _i64, _vp, _i64, ctypes.POINTER(ExecOptions), _pd, _pd]

@@ -18,6 +18,27 @@ namespace qi {
 
 constexpr int kSimtThreads = 256;
 
+// Rows [r0, r1) of U times the column `in`, written to column j of the tile.
+template <typename T, int R>
+__device__ __forceinline__ void column_rows(const typename Cx<T>::V2 *sm_mat, const typename Cx<T>::V2 (&in)[R], int r0,
+                                            int r1, typename Cx<T>::V2 *S, const TileGeom &g, int j) {
+    using V2 = typename Cx<T>::V2;
+#pragma unroll 1
+    for (int ro = r0; ro < r1; ++ro) {
+        const V2 *mrow = sm_mat + ro * R;
+        T ax = 0, ay = 0;
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            const V2 m = mrow[r];
+            ax = ::fma(m.x, in[r].x, ax);
+            ax = ::fma(-m.y, in[r].y, ax);
+            ay = ::fma(m.x, in[r].y, ay);
+            ay = ::fma(m.y, in[r].x, ay);
+        }
+        S[tile_sidx(g, ro, j)] = Cx<T>::make(ax, ay);
+    }
+}
+
 // Fused block on CUDA cores.  Persistent CTAs walk the tiles; tile t + 2*grid
 // is prefetched with cp.async into the buffer tile t just released, so loads
 // overlap the matrix-vector work of the other buffer.  Each column's 2^K
@@ -60,29 +81,19 @@ __global__ void __launch_bounds__(kSimtThreads) k_fused_simt(typename Cx<T>::V2 
         V2 *S = (it & 1) ? S1 : S0;
         cp_async_wait<1>();
         __syncthreads();
-        if (computes) {
-            for (int j = col0; j < ncol; j += kSimtThreads) {
-                V2 in[R];
+        // Every thread runs the same number of column steps and reaches every
+        // barrier: the computing threads can share a warp with idle ones when a
+        // tile has fewer than 32 amplitudes.
+        for (int j0 = 0; j0 < ncol; j0 += kSimtThreads) {
+            const int j = j0 + col0;
+            const bool act = computes && j < ncol;
+            V2 in[R];
+            if (act) {
 #pragma unroll
                 for (int r = 0; r < R; ++r) in[r] = S[tile_sidx(g, r, j)];
-                if (split > 1) __syncthreads();   // every slice has read the column
-#pragma unroll 1
-                for (int ro = part * rows_per; ro < (part + 1) * rows_per; ++ro) {
-                    const V2 *mrow = sm_mat + ro * R;
-                    T ax = 0, ay = 0;
-#pragma unroll
-                    for (int r = 0; r < R; ++r) {
-                        const V2 m = mrow[r];
-                        ax = ::fma(m.x, in[r].x, ax);
-                        ax = ::fma(-m.y, in[r].y, ax);
-                        ay = ::fma(m.x, in[r].y, ay);
-                        ay = ::fma(m.y, in[r].x, ay);
-                    }
-                    S[tile_sidx(g, ro, j)] = Cx<T>::make(ax, ay);
-                }
             }
-        } else if (split > 1) {
-            __syncthreads();   // match the barrier of the computing threads
+            if (split > 1) __syncthreads();   // every row slice has read the column
+            if (act) column_rows<T, R>(sm_mat, in, part * rows_per, (part + 1) * rows_per, S, g, j);
         }
         __syncthreads();
         tile_store(g, w, tab, a, tile_base(g, t), S);

@@ -50,7 +50,11 @@ namespace qi {
 constexpr int kConvWarps = 8, kEpiWarps = 4;
 constexpr int kProducerWarp = kConvWarps + kEpiWarps, kMmaWarp = kProducerWarp + 1;
 constexpr int kTcThreads = (kMmaWarp + 1) * 32;   // 448
-constexpr uint32_t kWaitLimit = 1u << 22;   // bounded mbarrier wait (iterations of try_wait)
+// Every mbarrier wait gives up after kWaitNs of wall time (%globaltimer), or after
+// kWaitLimit polls should the timer not advance; a single try_wait may suspend
+// the thread for a hardware-defined time, so the clock is the real bound.
+constexpr uint64_t kWaitNs = 2000000000ull;   // 2 s
+constexpr uint32_t kWaitLimit = 1u << 26;
 
 // ---------------------------------------------------------- PTX wrappers --
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -71,10 +75,20 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
     return ok != 0;
 }
 
-// Bounded wait: false if the phase did not complete within kWaitLimit tries.
+__device__ __forceinline__ uint64_t global_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Bounded wait: false if the phase did not complete within kWaitNs.
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity) {
-    for (uint32_t i = 0; i < kWaitLimit; ++i)
+    if (mbar_try_wait(bar, parity)) return true;
+    const uint64_t t0 = global_ns();
+    for (uint32_t i = 0; i < kWaitLimit; ++i) {
         if (mbar_try_wait(bar, parity)) return true;
+        if ((i & 31u) == 31u && global_ns() - t0 > kWaitNs) return false;
+    }
     return false;
 }
 
@@ -212,9 +226,14 @@ __device__ __forceinline__ void bulk_load(void *dst, const void *src, uint32_t b
 // Bounded wait that also gives up when another role raised the abort flag;
 // a timeout raises it and records status 2 in the state's error flag.
 __device__ __forceinline__ bool wait_or_abort(uint64_t *bar, uint32_t parity, volatile int *abort_flag, int *err_flag) {
+    if (mbar_try_wait(bar, parity)) return true;
+    const uint64_t t0 = global_ns();
     for (uint32_t i = 0; i < kWaitLimit; ++i) {
         if (mbar_try_wait(bar, parity)) return true;
-        if ((i & 31u) == 31u && *abort_flag) return false;
+        if ((i & 31u) == 31u) {
+            if (*abort_flag) return false;
+            if (global_ns() - t0 > kWaitNs) break;
+        }
     }
     *abort_flag = 1;
     atomicExch(err_flag, 2);   // 2 = a bounded device wait ran out (1 is ZeroNorm)
@@ -343,7 +362,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_fused_tc(float2 *a, const flo
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = *tmem_slot;
-    const uint64_t ntiles = g.ntiles, t0 = blockIdx.x, tstep = gridDim.x;
+    // tile counts stay below 2^32 (2^(n-13) tiles for n <= 44)
+    const uint32_t ntiles = (uint32_t)g.ntiles, t0 = blockIdx.x, tstep = gridDim.x;
     const bool pair_rows = !g.q0_is_col;   // qubit 0 is target 0: rows r, r+1 are adjacent amplitudes
 
     if (warp < kConvWarps) {
@@ -353,7 +373,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_fused_tc(float2 *a, const flo
         const uint32_t lane_base = (uint32_t)(quarter * 32) << 16;
         const int r0 = slice * C::CONV_ROWS;
         int it = 0;
-        for (uint64_t t = t0; t < ntiles; t += tstep, ++it) {
+        for (uint32_t t = t0; t < ntiles; t += tstep, ++it) {
             const int b = it % NB;
             if (!warp_wait_or_abort(raw_full + b, (uint32_t)(it / NB) & 1u, abort_flag, err_flag)) break;
             const float2 *S = reinterpret_cast<const float2 *>(tiles + (size_t)b * C::TILE_BYTES);
@@ -410,7 +430,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_fused_tc(float2 *a, const flo
         const uint64_t cx = tile_colx(g, (uint32_t)(quarter * 32 + lane));
         const uint32_t lane_base = (uint32_t)(quarter * 32) << 16;
         int it = 0;
-        for (uint64_t t = t0; t < ntiles; t += tstep, ++it) {
+        for (uint32_t t = t0; t < ntiles; t += tstep, ++it) {
             const int d = it & 1;
             if (!warp_wait_or_abort(d_full + d, (uint32_t)(it >> 1) & 1u, abort_flag, err_flag)) break;
             tc_fence_after();
@@ -446,7 +466,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_fused_tc(float2 *a, const flo
             const uint32_t run_bytes = (uint32_t)sizeof(float2) << g.L;
             const int nruns = 1 << g.nhigh;
             int it = 0, issued = 0;
-            for (uint64_t t = t0; t < ntiles; t += tstep, ++it) {
+            for (uint32_t t = t0; t < ntiles; t += tstep, ++it) {
                 const int b = it % NB;
                 if (it >= NB && !wait_or_abort(raw_empty + b, (uint32_t)(it / NB - 1) & 1u, abort_flag, err_flag))
                     break;
@@ -471,7 +491,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_fused_tc(float2 *a, const flo
             constexpr uint32_t idesc = tf32_idesc(128, 2 * R);
             int it = 0;
             bool ok = true;
-            for (uint64_t t = t0; ok && t < ntiles; t += tstep, ++it) {
+            for (uint32_t t = t0; ok && t < ntiles; t += tstep, ++it) {
                 const int d = it & 1;
                 if (it >= 2 && !wait_or_abort(d_empty + d, (uint32_t)((it >> 1) - 1) & 1u, abort_flag, err_flag))
                     break;

@@ -565,6 +565,10 @@ Status launch_op(qi_state *s, const Op &op, const void *d_mats, const void *d_tc
         const char *mp = (const char *)d_mats + (size_t)op.mat_offset * esz;
         return launch_diagk(s, op.k, op.targets, mp);
     }
+    case OP_PHASE_POLY: {
+        if (!d_tc || op.tc_offset < 0) return err(QI_ERR_UNKNOWN, op.kind, -1, "phase polynomial without its block");
+        return launch_phase_poly(s, (const float *)d_tc + op.tc_offset);
+    }
     default:
         return err(QI_ERR_UNKNOWN, op.kind, -1, "unknown op");
     }

@@ -3,6 +3,7 @@
 
 #include <cuda_runtime.h>
 #include <atomic>
+#include <complex>
 #include <cstdint>
 #include <cstring>
 #include <mutex>
@@ -91,6 +92,7 @@ enum OpKind : int32_t {
     OP_PAULI_NORM = 6,    // P psi then normalise (Gate::PauliString)
     OP_DIAGK = 7,         // diagonal on k targets (2^k phases), controlled by nothing
     OP_NORMALISE = 8,     // FP64 norm on the device, divide (periodic renormalisation)
+    OP_PHASE_POLY = 9,    // run of diagonal blocks as one quadratic phase polynomial over all qubits (FP32)
 };
 enum Mat1Mode : int32_t { M1_GENERAL = 0, M1_DIAG = 1, M1_ANTIDIAG = 2, M1_PHASE1 = 3, M1_REAL = 4 };
 
@@ -143,10 +145,36 @@ Status launch_fused(qi_state *s, int k, const int32_t *targets, const void *d_ma
 // 3xTF32 tcgen05 kernel (FP32 states, k = 5 or 6, n >= k + 7); d_tc holds the
 // six operand blocks prepared by tc_blocks().
 Status launch_fused_tc(qi_state *s, int k, const int32_t *targets, const void *d_tc);
-// Host: the six K-major operand blocks {Re U, Im U, -Im U} x {tf32 hi, lo}
+// Host: the six K-major operand blocks {-Im U, Re U, Im U} x {tf32 hi, lo}
 // (each 2^k x 2^k floats in the no-swizzle core-matrix layout) of a fused
 // matrix U (row-major complex, FP64).  Appends 6 * 4^k floats to `out`.
 void tc_blocks(int k, const double *U, std::vector<float> &out);
 Status launch_diagk(qi_state *s, int k, const int32_t *targets, const void *d_phases);
+
+// ------------------------------------------------------------ phase poly --
+// A diagonal operator exp(2 pi i f(x)) with f a polynomial of degree <= 2 in
+// the amplitude-index bits x_q: f = c0 + sum_q a[q] x_q + sum_{q<r} b[q][r] x_q x_r.
+// Coefficients are fixed-point turns (2^64 = one turn), so sums wrap mod 2 pi exactly.
+struct PhasePoly {
+    int n = 0;
+    uint64_t c0 = 0;
+    std::vector<uint64_t> a;   // n
+    std::vector<uint64_t> b;   // n * n, b[q * n + r] for q < r
+    void init(int nq) {
+        n = nq;
+        c0 = 0;
+        a.assign((size_t)nq, 0);
+        b.assign((size_t)nq * nq, 0);
+    }
+};
+// Add the phase polynomial of a diagonal table over `qubits` (phases[x], bit j
+// of x <-> qubits[j]) to pp.  False (pp unchanged) if an entry is not of unit
+// modulus or the table has terms of degree > 2.
+bool phase_poly_add_table(PhasePoly &pp, int k, const int32_t *qubits, const std::complex<double> *phases);
+// Iteration bits h of the phase-polynomial kernel for n qubits (FP32 states).
+int phase_poly_iter_bits(int n);
+// Device block of pp (32-bit words) appended to `out`, padded to 16 bytes.
+void phase_poly_device_block(const PhasePoly &pp, std::vector<float> &out);
+Status launch_phase_poly(qi_state *s, const void *d_block);
 
 }  // namespace qi

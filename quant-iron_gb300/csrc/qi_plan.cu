@@ -205,6 +205,7 @@ Status build_plan(qi_plan *p, std::vector<Elem> &elems) {
     p->ops.clear();
     p->mats.clear();
     p->tc.clear();
+    p->polys.clear();
     int tc_blocks_since = 0, tc_total = 0;
     std::fill(std::begin(p->stats.n_blocks_by_k), std::end(p->stats.n_blocks_by_k), 0);
     p->stats.n_gates = (int64_t)elems.size();
@@ -256,9 +257,37 @@ Status build_plan(qi_plan *p, std::vector<Elem> &elems) {
             });
         }
         for (auto &t : th) t.join();
+        // FP32 plans: a run of consecutive diagonal blocks whose phases are
+        // polynomials of degree <= 2 is applied as one phase polynomial (one pass).
+        const bool poly_ok = p->prec == QI_F32;
+        PhasePoly pending;
+        std::vector<Op> pending_ops;
+        if (poly_ok) pending.init(n);
+        auto flush = [&]() {
+            if (pending_ops.size() >= 2) {
+                Op op;
+                op.kind = OP_PHASE_POLY;
+                op.k = (int32_t)pending_ops.size();
+                for (const Op &d : pending_ops)
+                    for (int j = 0; j < d.k; ++j) op.zmask |= 1ull << d.targets[j];
+                op.mat_offset = (int64_t)p->polys.size();
+                op.tc_offset = (int64_t)p->tc.size();
+                phase_poly_device_block(pending, p->tc);
+                p->polys.push_back(pending);
+                p->ops.push_back(op);
+            } else if (pending_ops.size() == 1) {
+                p->ops.push_back(pending_ops[0]);
+            }
+            pending_ops.clear();
+            if (poly_ok) pending.init(n);
+        };
         for (size_t bi = 0; bi < blocks.size(); ++bi) {
             const Block &b = blocks[bi];
-            if (b.single) { lower_single(elems[b.members[0]]); continue; }
+            if (b.single) {
+                flush();
+                lower_single(elems[b.members[0]]);
+                continue;
+            }
             bool diag = true;
             for (int idx : b.members) diag = diag && elems[idx].diagonal;
             const int k = (int)qb[bi].size();
@@ -269,8 +298,17 @@ Status build_plan(qi_plan *p, std::vector<Elem> &elems) {
             const int dim = 1 << k;
             if (diag) {
                 op.kind = OP_DIAGK;
-                for (int r = 0; r < dim; ++r) p->mats.push_back(mb[bi][(size_t)r * dim + r]);
+                std::vector<cd> table((size_t)dim);
+                for (int r = 0; r < dim; ++r) table[(size_t)r] = mb[bi][(size_t)r * dim + r];
+                p->mats.insert(p->mats.end(), table.begin(), table.end());
+                if (poly_ok && phase_poly_add_table(pending, k, op.targets, table.data())) {
+                    pending_ops.push_back(op);
+                    p->stats.n_blocks_by_k[k]++;
+                    continue;
+                }
+                flush();
             } else {
+                flush();
                 op.kind = OP_FUSED;
                 op.mode = use_tc;
                 for (size_t i = 0; i < (size_t)dim * dim; ++i) p->mats.push_back(mb[bi][i]);
@@ -292,6 +330,7 @@ Status build_plan(qi_plan *p, std::vector<Elem> &elems) {
                 }
             }
         }
+        flush();
     }
     // Tensor-core accumulation rounds toward zero: renormalise once at the end
     // (unless disabled, or the last op already did).
@@ -522,6 +561,19 @@ qi_status qi_apply_matrix(qi_state *s, const int32_t *targets, int32_t k, const 
 qi_status qi_plan_num_ops(const qi_plan *p, int64_t *out) {
     if (!p || !out) return publish(err(QI_ERR_NULL_ARGUMENT));
     *out = (int64_t)p->ops.size();
+    return publish(ok_status());
+}
+
+qi_status qi_plan_op_phase_poly(const qi_plan *p, int64_t i, uint64_t *c0, uint64_t *a, uint64_t *b) {
+    if (!p || !c0 || !a || !b) return publish(err(QI_ERR_NULL_ARGUMENT));
+    if (i < 0 || i >= (int64_t)p->ops.size()) return publish(err(QI_ERR_INVALID_INPUT_VALUE, i));
+    const Op &op = p->ops[(size_t)i];
+    if (op.kind != OP_PHASE_POLY || op.mat_offset < 0 || op.mat_offset >= (int64_t)p->polys.size())
+        return publish(err(QI_ERR_INVALID_INPUT_VALUE, i, op.kind, "not a phase-polynomial op"));
+    const PhasePoly &pp = p->polys[(size_t)op.mat_offset];
+    *c0 = pp.c0;
+    std::copy(pp.a.begin(), pp.a.end(), a);
+    std::copy(pp.b.begin(), pp.b.end(), b);
     return publish(ok_status());
 }
 

@@ -37,8 +37,10 @@ struct qi_plan {
     std::vector<qi::Op> ops;
     std::vector<std::complex<double>> mats;   // block matrices / phase tables (host copy, FP64)
     void *d_mats = nullptr;                   // same, in the plan's precision
-    std::vector<float> tc;                    // tensor-core operand blocks of FP32 fused ops (k >= 5)
+    std::vector<float> tc;                    // FP32 device blocks: tensor-core operands (fused ops, k >= 5)
+                                              // and phase-polynomial blocks, as raw 32-bit words
     void *d_tc = nullptr;
+    std::vector<qi::PhasePoly> polys;         // host copy of each OP_PHASE_POLY op (op.mat_offset indexes it)
     qi_plan_stats stats = {};
     std::vector<qi::Block> partition_override;   // set by callers that chose the partition
 };

@@ -25,6 +25,7 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <cstdint>
+#include <cstring>
 
 namespace qi {
 

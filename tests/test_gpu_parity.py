@@ -123,6 +123,19 @@ def test_random_circuit_fused(qi, orc, n, prec, k):
         assert infidelity(got, want) < 1e-6
 
 
+@pytest.mark.parametrize("prec", [0, 1], ids=["f64", "f32"])
+@pytest.mark.parametrize("n", [1, 2, 3, 4, 5])
+def test_small_states_fused(qi, orc, n, prec):
+    """Tiles smaller than a warp (2^n < 32 amplitudes): the CUDA-core block
+    kernel's barriers are reached by every thread of the CTA."""
+    gates = workloads.random_circuit(n, layers=4, seed=200 + n)
+    init = orc.execute(workloads.plus_state(n), n, workloads.random_circuit(n, 1, seed=n, with_qft=False))
+    want = orc.execute(init, n, gates)
+    for k in range(1, min(n, 5) + 1):
+        got = run(qi, n, prec, init, gates, fusion=qi.FUSION_GREEDY, k=k)
+        assert np.max(np.abs(got - want)) < (1e-12 if prec == 0 else 2e-6), (n, k)
+
+
 def test_config0_20q_full(qi, orc):
     """Config 0: 20 qubits, |+>^20, 40 layers + QFT (1400 gates), <H> of the open-chain Heisenberg."""
     n = 20

@@ -31,6 +31,22 @@ def _apply_local(state, n, targets, mat, cmask=0):
     return np.transpose(res, inv).reshape(-1)
 
 
+def poly_phases(poly, n):
+    """exp(2 pi i f(x) / 2^64) for every index x (uint64 arithmetic wraps like the engine's)."""
+    c0, a, b = poly
+    x = np.arange(1 << n, dtype=np.uint64)
+    bits = [((x >> np.uint64(q)) & np.uint64(1)) for q in range(n)]
+    f = np.full(1 << n, c0, dtype=np.uint64)
+    with np.errstate(over="ignore"):
+        for q in range(n):
+            f += bits[q] * a[q]
+            for r in range(q + 1, n):
+                if b[q, r]:
+                    f += (bits[q] & bits[r]) * b[q, r]
+    turns = f.astype(np.float64) / 2.0 ** 64
+    return np.exp(2j * np.pi * turns)
+
+
 def replay(ops, n, init):
     s = init.astype(np.complex128).copy()
     for op in ops:
@@ -47,6 +63,10 @@ def replay(ops, n, init):
             s = _apply_local(s, n, op["targets"], op["matrix"], 0)
         elif kind == 7:
             s = _apply_local(s, n, op["targets"], np.diag(op["matrix"]).reshape(-1), 0)
+        elif kind == 9:
+            s = s * poly_phases(op["poly"], n)
+        elif kind == 8:
+            s = s / np.linalg.norm(s)
         elif kind == 5:
             x, z = op["xmask"], op["zmask"]
             ch, sh = op["matrix"][0], op["matrix"][1]
@@ -129,3 +149,69 @@ def test_qft_diagonal_runs_fuse(qi):
     gates = workloads.qft(workloads.GateList(), list(range(n))).array()
     st = qi.Plan(n, qi.F32, gates, fusion=qi.FUSION_GREEDY, max_block_qubits=6).stats()
     assert st["n_kernels"] < len(gates) / 3
+
+
+def diag_mix(n, seed, layers=3):
+    """QFT ladders plus random diagonal gates (RZ, S, T, P, CZ, controlled phases) between H layers."""
+    from quant_iron_gb300.workloads import GateList
+    rng = np.random.default_rng(seed)
+    gl = GateList()
+    for _ in range(layers):
+        for q in range(n):
+            gl.add("H", [q])
+        for _ in range(4 * n):
+            a, b = (int(v) for v in rng.choice(n, 2, replace=False))
+            kind = rng.integers(0, 6)
+            if kind == 0:
+                gl.add("RZ", [a], [], [rng.uniform(-3, 3)])
+            elif kind == 1:
+                gl.add("S", [a])
+            elif kind == 2:
+                gl.add("T", [a], [b])
+            elif kind == 3:
+                gl.add("P", [a], [b], [rng.uniform(-3, 3)])
+            elif kind == 4:
+                gl.add("Z", [a], [b])
+            else:
+                gl.add("RZ", [a], [b], [rng.uniform(-3, 3)])
+    workloads.qft(gl, list(range(n)))
+    return gl.array()
+
+
+@pytest.mark.parametrize("seed", [0, 1])
+def test_fp32_diagonal_runs_become_phase_polynomials(qi, orc, seed):
+    n = 9
+    gates = diag_mix(n, seed)
+    init = workloads.plus_state(n)
+    want = orc.execute(init, n, gates)
+    plan = qi.Plan(n, qi.F32, gates, fusion=qi.FUSION_GREEDY, max_block_qubits=4)
+    ops = plan.ops()
+    polys = [op for op in ops if op["kind"] == 9]
+    assert polys and all(op["k"] >= 2 for op in polys)
+    got = replay(ops, n, init)
+    assert np.max(np.abs(got - want)) < 1e-12
+    # FP64 plans keep one diagonal kernel per block
+    assert all(op["kind"] != 9 for op in qi.Plan(n, qi.F64, gates, fusion=qi.FUSION_GREEDY,
+                                                  max_block_qubits=4).ops())
+
+
+def test_phase_polynomial_rejects_degree_three(qi, orc):
+    """A doubly controlled phase has an x_a x_b x_c term: its block stays a diagonal table."""
+    from quant_iron_gb300.workloads import GateList
+    n = 8
+    gl = GateList()
+    gl.add("P", [0], [1], [0.7])
+    gl.add("RZ", [5], [6], [0.3])
+    gl.add("P", [2], [3, 4], [1.1])   # degree 3
+    gl.add("S", [3], [2])
+    gl.add("Z", [7], [0])
+    gl.add("P", [6], [7], [0.4])
+    gates = gl.array()
+    init = orc.execute(workloads.plus_state(n), n, workloads.random_circuit(n, 2, seed=3, with_qft=False))
+    plan = qi.Plan(n, qi.F32, gates, fusion=qi.FUSION_GREEDY, max_block_qubits=3)
+    ops = plan.ops()
+    # the degree-2 gates commute into one polynomial; the {2, 3, 4} block stays a table
+    assert [op["kind"] for op in ops] == [9, 7]
+    assert ops[1]["targets"] == [2, 3, 4]
+    got = replay(ops, n, init)
+    assert np.max(np.abs(got - orc.execute(init, n, gates))) < 1e-12

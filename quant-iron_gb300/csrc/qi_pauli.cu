@@ -236,6 +236,198 @@ __global__ void __launch_bounds__(256) k_group_expect(const typename Cx<T>::V2 *
     }
 }
 
+// ---- FP32 states: products and per-thread sums in FP32, folded into FP64
+// every kExpBatch elements, so a pass is bound by memory rather than by the
+// FP64 pipe (FP64 arithmetic runs at a small fraction of the FP32 rate here).
+constexpr int kExpBatch = 32, kExpUnroll = 4;
+constexpr int kExpLog2Threads = 18;   // diagonal group: 2^18 threads (1024 blocks of 256)
+
+struct TermF {   // a GroupTerm with its coefficient rounded to FP32 once per block
+    uint64_t zmask;
+    float re, im;
+};
+__device__ __forceinline__ TermF term_f32(const GroupTerm &g) { return TermF{g.zmask, (float)g.re, (float)g.im}; }
+
+template <int N>
+__device__ __forceinline__ float2 factor_f32(const TermF *t, uint64_t i) {
+    float re = 0.0f, im = 0.0f;
+#pragma unroll
+    for (int k = 0; k < N; ++k) {
+        const float sgn = (__popcll(i & t[k].zmask) & 1) ? -1.0f : 1.0f;
+        re = fmaf(sgn, t[k].re, re);
+        im = fmaf(sgn, t[k].im, im);
+    }
+    return make_float2(re, im);
+}
+__device__ __forceinline__ float2 factor_f32_n(const TermF *t, int n, uint64_t i) {
+    float re = 0.0f, im = 0.0f;
+    for (int k = 0; k < n; ++k) {
+        const float sgn = (__popcll(i & t[k].zmask) & 1) ? -1.0f : 1.0f;
+        re = fmaf(sgn, t[k].re, re);
+        im = fmaf(sgn, t[k].im, im);
+    }
+    return make_float2(re, im);
+}
+
+// Diagonal group (xmask = 0): sum_i |psi_i|^2 f(i).  With i = it * 2^s + tid,
+// f(i) = F(tid) [terms whose Z bits lie below s] + G[it] [terms above s, a
+// host table] + the straddling terms, evaluated per element.
+// NM = number of straddling terms held in registers (-1: runtime count nmix, read from shared memory).
+template <int NM>
+__global__ void __launch_bounds__(256) k_diag_expect_f32(const float2 *a, int s, int h, const float2 *G,
+                                                         const GroupTerm *terms, int nlo, int nmix, double *partials) {
+    constexpr int NR = NM > 0 ? NM : 1;
+    extern __shared__ TermF st_terms[];
+    for (int k = threadIdx.x; k < nlo + nmix; k += blockDim.x) st_terms[k] = term_f32(terms[k]);
+    __syncthreads();
+    const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
+    const float2 F = factor_f32_n(st_terms, nlo, tid);
+    const TermF *mix = st_terms + nlo;
+    // straddling terms: sign = (low part of the sign, fixed per thread) x (high part, per iteration)
+    uint32_t zh[NR];
+    float mr[NR], mi[NR];
+#pragma unroll
+    for (int k = 0; k < NR; ++k) {
+        if (NM > 0) {
+            const bool sl = __popcll((uint64_t)tid & mix[k].zmask) & 1;
+            zh[k] = (uint32_t)(mix[k].zmask >> s);
+            mr[k] = sl ? -mix[k].re : mix[k].re;
+            mi[k] = sl ? -mix[k].im : mix[k].im;
+        }
+    }
+    const uint32_t iters = 1u << h;
+    double dr = 0.0, di = 0.0;
+    float br = 0.0f, bi = 0.0f;
+    constexpr int U = 2 * kExpUnroll;
+    for (uint32_t it0 = 0; it0 < iters; it0 += U) {
+        float2 v[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+            if (it0 + u < iters) v[u] = ldg_stream(a + ((((uint64_t)(it0 + u)) << s) | tid));
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const uint32_t it = it0 + u;
+            if (it >= iters) break;
+            const float2 g = __ldg(G + it);
+            float fr = F.x + g.x, fi = F.y + g.y;
+            if (NM > 0) {
+#pragma unroll
+                for (int k = 0; k < NR; ++k) {
+                    const bool sh = __popc(it & zh[k]) & 1;
+                    fr += sh ? -mr[k] : mr[k];
+                    fi += sh ? -mi[k] : mi[k];
+                }
+            } else if (nmix > 0) {
+                const float2 f = factor_f32_n(mix, nmix, ((uint64_t)it << s) | tid);
+                fr += f.x;
+                fi += f.y;
+            }
+            const float p = fmaf(v[u].x, v[u].x, v[u].y * v[u].y);
+            br = fmaf(p, fr, br);
+            bi = fmaf(p, fi, bi);
+        }
+        if (((it0 / U) & (kExpBatch / U - 1)) == kExpBatch / U - 1) {
+            dr += br;
+            di += bi;
+            br = bi = 0.0f;
+        }
+    }
+    dr += br;
+    di += bi;
+    const double r0 = block_sum(dr), r1 = block_sum(di);
+    if (threadIdx.x == 0) {
+        partials[blockIdx.x * 4 + 0] = r0;
+        partials[blockIdx.x * 4 + 1] = r1;
+    }
+}
+
+// Group with xmask != 0: pairs (i, i ^ x), i with bit h (the top bit of x) clear:
+// conj(psi_i) f(i) psi_j + conj(psi_j) f(j) psi_i.  Terms with Z mask 0 are the
+// constant c0; the other N terms (N = 0: runtime count cnt) are held in
+// registers, and the sign of a term at j = i ^ x is its sign at i times
+// (-1)^popc(x & z).  IDX is the index type (uint32_t for n <= 32).
+template <int N, typename IDX>
+__global__ void __launch_bounds__(256) k_xgroup_expect_f32(const float2 *a, uint64_t npairs, uint64_t xmask, float c0r,
+                                                           float c0i, const GroupTerm *terms, int cnt,
+                                                           double *partials) {
+    constexpr int NR = N > 0 ? N : 1;
+    extern __shared__ TermF st_terms[];
+    for (int k = threadIdx.x; k < cnt; k += blockDim.x) st_terms[k] = term_f32(terms[k]);
+    __syncthreads();
+    IDX z[NR];
+    float cr_[NR], ci_[NR];
+    bool px[NR];
+#pragma unroll
+    for (int k = 0; k < NR; ++k) {
+        if (N > 0) {
+            z[k] = (IDX)st_terms[k].zmask;
+            cr_[k] = st_terms[k].re;
+            ci_[k] = st_terms[k].im;
+            px[k] = (__popcll(xmask & st_terms[k].zmask) & 1) != 0;
+        }
+    }
+    const int h = 63 - __clzll(xmask);
+    const IDX lo_mask = (IDX)((1ull << h) - 1), xm = (IDX)xmask;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    double dr = 0.0, di = 0.0;
+    float br = 0.0f, bi = 0.0f;
+    int batch = 0;
+    for (uint64_t w0 = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; w0 < npairs; w0 += stride * kExpUnroll) {
+        float2 x[kExpUnroll], y[kExpUnroll];
+        IDX iv[kExpUnroll];
+#pragma unroll
+        for (int u = 0; u < kExpUnroll; ++u) {
+            const uint64_t w = w0 + u * stride;
+            const IDX ww = (IDX)w;
+            iv[u] = ((ww & ~lo_mask) << 1) | (ww & lo_mask);
+            if (w < npairs) {
+                x[u] = ldg_stream(a + iv[u]);
+                y[u] = ldg_stream(a + (iv[u] ^ xm));
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < kExpUnroll; ++u) {
+            if (w0 + u * stride >= npairs) break;
+            const IDX i = iv[u];
+            float fir = c0r, fii = c0i, fjr = c0r, fji = c0i;
+            if (N > 0) {
+#pragma unroll
+                for (int k = 0; k < NR; ++k) {
+                    const bool si = (sizeof(IDX) == 4 ? __popc((uint32_t)(i & z[k])) : __popcll((uint64_t)(i & z[k]))) & 1;
+                    const bool sj = si != px[k];
+                    fir += si ? -cr_[k] : cr_[k];
+                    fii += si ? -ci_[k] : ci_[k];
+                    fjr += sj ? -cr_[k] : cr_[k];
+                    fji += sj ? -ci_[k] : ci_[k];
+                }
+            } else {
+                const float2 fi = factor_f32_n(st_terms, cnt, i), fj = factor_f32_n(st_terms, cnt, i ^ xm);
+                fir += fi.x;
+                fii += fi.y;
+                fjr += fj.x;
+                fji += fj.y;
+            }
+            // c = conj(x) y;  fi c + fj conj(c)
+            const float cr = fmaf(x[u].x, y[u].x, x[u].y * y[u].y), ci = fmaf(x[u].x, y[u].y, -x[u].y * y[u].x);
+            br += (fir * cr - fii * ci) + (fjr * cr + fji * ci);
+            bi += (fir * ci + fii * cr) + (fji * cr - fjr * ci);
+        }
+        if (++batch == kExpBatch / kExpUnroll) {
+            dr += br;
+            di += bi;
+            br = bi = 0.0f;
+            batch = 0;
+        }
+    }
+    dr += br;
+    di += bi;
+    const double r0 = block_sum(dr), r1 = block_sum(di);
+    if (threadIdx.x == 0) {
+        partials[blockIdx.x * 4 + 0] = r0;
+        partials[blockIdx.x * 4 + 1] = r1;
+    }
+}
+
 // acc[0..1] += fixed-order sum of the partials (one thread block).
 __global__ void k_accumulate(const double *partials, int nb, double *acc) {
     for (int c = 0; c < 2; ++c) {
@@ -320,7 +512,94 @@ Status sumop_expectation(qi_state *s, const qi_pauli_term *terms, int64_t nt, do
     if (!st.ok()) return st;
     QI_CUDA(cudaMemsetAsync(s->d_result, 0, 2 * sizeof(double), s->stream));
     const bool f32 = s->prec == QI_F32;
+    std::vector<void *> scratch;   // per-call device tables, freed (stream-ordered) at the end
     for (const GroupHdr &h : hdrs) {
+        if (f32 && (size_t)h.count * sizeof(GroupTerm) <= 48 * 1024) {
+            const GroupTerm *gt = gts.data() + h.first;
+            unsigned nb = 1;
+            if (h.xmask == 0) {
+                // split the Z terms at the thread bits: below sb, above sb, straddling
+                const int n = s->n, sb = std::min(n, kExpLog2Threads), hb = n - sb;
+                const uint64_t lo = (sb >= 64) ? ~0ull : ((1ull << sb) - 1);
+                std::vector<GroupTerm> lm;
+                std::vector<const GroupTerm *> hi;
+                int nlo = 0;
+                for (int k = 0; k < h.count; ++k)
+                    if ((gt[k].zmask & ~lo) == 0) { lm.insert(lm.begin() + nlo, gt[k]); ++nlo; }
+                for (int k = 0; k < h.count; ++k)
+                    if ((gt[k].zmask & lo) == 0 && (gt[k].zmask & ~lo) != 0) hi.push_back(&gt[k]);
+                    else if ((gt[k].zmask & lo) != 0 && (gt[k].zmask & ~lo) != 0) lm.push_back(gt[k]);
+                const int nmix = (int)lm.size() - nlo;
+                std::vector<float2> G((size_t)1 << hb);
+                for (uint64_t it = 0; it < G.size(); ++it) {
+                    double re = 0.0, im = 0.0;
+                    for (const GroupTerm *t : hi) {
+                        const double sgn = (__builtin_popcountll((it << sb) & t->zmask) & 1) ? -1.0 : 1.0;
+                        re += sgn * t->re;
+                        im += sgn * t->im;
+                    }
+                    G[it] = make_float2((float)re, (float)im);
+                }
+                void *dG = nullptr, *dT = nullptr;
+                QI_CUDA(cudaMallocAsync(&dG, G.size() * sizeof(float2), s->stream));
+                QI_CUDA(cudaMallocAsync(&dT, std::max<size_t>(1, lm.size()) * sizeof(GroupTerm), s->stream));
+                scratch.push_back(dG);
+                scratch.push_back(dT);
+                QI_CUDA(cudaMemcpyAsync(dG, G.data(), G.size() * sizeof(float2), cudaMemcpyHostToDevice, s->stream));
+                if (!lm.empty())
+                    QI_CUDA(cudaMemcpyAsync(dT, lm.data(), lm.size() * sizeof(GroupTerm), cudaMemcpyHostToDevice, s->stream));
+                const uint64_t threads = 1ull << sb;
+                const unsigned tpb = (unsigned)std::min<uint64_t>(threads, 256);
+                nb = (unsigned)(threads / tpb);
+                const size_t smd = std::max<size_t>(1, lm.size()) * sizeof(GroupTerm);
+                const float2 *amp = (const float2 *)s->amps;
+                const GroupTerm *dtt = (const GroupTerm *)dT;
+                switch (nmix) {
+                case 0: k_diag_expect_f32<0><<<nb, tpb, smd, s->stream>>>(amp, sb, hb, (const float2 *)dG, dtt, nlo, nmix, s->d_partials); break;
+                case 1: k_diag_expect_f32<1><<<nb, tpb, smd, s->stream>>>(amp, sb, hb, (const float2 *)dG, dtt, nlo, nmix, s->d_partials); break;
+                case 2: k_diag_expect_f32<2><<<nb, tpb, smd, s->stream>>>(amp, sb, hb, (const float2 *)dG, dtt, nlo, nmix, s->d_partials); break;
+                case 3: k_diag_expect_f32<3><<<nb, tpb, smd, s->stream>>>(amp, sb, hb, (const float2 *)dG, dtt, nlo, nmix, s->d_partials); break;
+                default: k_diag_expect_f32<-1><<<nb, tpb, smd, s->stream>>>(amp, sb, hb, (const float2 *)dG, dtt, nlo, nmix, s->d_partials);
+                }
+            } else {
+                // constant part (Z mask 0) on the host; the other terms packed for the kernel
+                double c0r = 0.0, c0i = 0.0;
+                std::vector<GroupTerm> nz;
+                for (int k = 0; k < h.count; ++k) {
+                    if (gt[k].zmask == 0) { c0r += gt[k].re; c0i += gt[k].im; }
+                    else nz.push_back(gt[k]);
+                }
+                void *dT = nullptr;
+                QI_CUDA(cudaMallocAsync(&dT, std::max<size_t>(1, nz.size()) * sizeof(GroupTerm), s->stream));
+                scratch.push_back(dT);
+                if (!nz.empty())
+                    QI_CUDA(cudaMemcpyAsync(dT, nz.data(), nz.size() * sizeof(GroupTerm), cudaMemcpyHostToDevice, s->stream));
+                const uint64_t npairs = s->dim() >> 1;
+                nb = (unsigned)std::min<uint64_t>(std::max<uint64_t>((npairs + 256 * kExpUnroll - 1) / (256 * kExpUnroll), 1),
+                                                  kReduceBlocks);
+                const size_t sm = std::max<size_t>(1, nz.size()) * sizeof(GroupTerm);
+                const GroupTerm *dt = (const GroupTerm *)dT;
+                const float2 *amp = (const float2 *)s->amps;
+                const int cnt = (int)nz.size();
+                const float fr = (float)c0r, fi = (float)c0i;
+#define QI_XG(NN, IDX)                                                                                               \
+    k_xgroup_expect_f32<NN, IDX><<<nb, 256, sm, s->stream>>>(amp, npairs, h.xmask, fr, fi, dt, cnt, s->d_partials)
+                const bool narrow = s->n <= 32;
+                switch (cnt) {
+                case 0: if (narrow) QI_XG(0, uint32_t); else QI_XG(0, uint64_t); break;
+                case 1: if (narrow) QI_XG(1, uint32_t); else QI_XG(1, uint64_t); break;
+                case 2: if (narrow) QI_XG(2, uint32_t); else QI_XG(2, uint64_t); break;
+                case 3: if (narrow) QI_XG(3, uint32_t); else QI_XG(3, uint64_t); break;
+                default: if (narrow) QI_XG(0, uint32_t); else QI_XG(0, uint64_t);
+                }
+#undef QI_XG
+            }
+            k_accumulate<<<1, 256, 0, s->stream>>>(s->d_partials, (int)nb, s->d_result);
+            count_launch(2);
+            st = check_launch(h.xmask ? "k_xgroup_expect_f32" : "k_diag_expect_f32");
+            if (!st.ok()) return st;
+            continue;
+        }
         const uint64_t work = h.xmask ? (s->dim() >> 1) : s->dim();
         uint64_t nb64 = (work + kReduceThreads - 1) / kReduceThreads;
         const unsigned nb = (unsigned)std::min<uint64_t>(std::max<uint64_t>(nb64, 1), kReduceBlocks);
@@ -337,6 +616,7 @@ Status sumop_expectation(qi_state *s, const qi_pauli_term *terms, int64_t nt, do
         if (!st.ok()) return st;
     }
     QI_CUDA(cudaMemcpyAsync(s->h_result, s->d_result, 2 * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+    for (void *p : scratch) QI_CUDA(cudaFreeAsync(p, s->stream));
     QI_CUDA(cudaFreeAsync(d_hdr, s->stream));
     QI_CUDA(cudaFreeAsync(d_terms, s->stream));
     QI_CUDA(cudaStreamSynchronize(s->stream));

@@ -354,8 +354,18 @@ def main():
                                 "share": round(v["ms"] / max(1e-9, sum(x["ms"] for x in by_kernel.values())), 4)}
                             for k, v in by_kernel.items()}}
 
-    # energy of the final state (FP64 reduction)
+    # energy of the final state (FP64 reduction), and the time of SumOp::expectation_value
     energy = qi.sumop_expectation(st, terms).real
+    ex_t = []
+    for _ in range(3):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        qi.sumop_expectation(st, terms)
+        ex_t.append(time.perf_counter() - t0)
+    n_groups = len({(int(t["xmask"])) for t in terms})
+    expectation = {"terms": len(terms), "x_groups": n_groups, "ms": min(ex_t) * 1e3,
+                   "passes_gbs": n_groups * (1 << n) * 8 / min(ex_t) / 1e9,
+                   "note": "one read pass of the FP32 state per X-mask group, host call to result (synchronous)"}
 
     extra = {}
     if rank == 0 and not args.skip_baselines:
@@ -402,6 +412,7 @@ def main():
                  "energy_error": abs(energy - energy64),
                  "gates_per_s_fused": len(gates) / (ms_per_step / 1e3)}
         extra["adjoint"] = adjoint_leg(qi, workloads, stream, torch, np)
+    extra["expectation"] = expectation
 
     # end-to-end through the public API with host buffers: H2D of the initial state,
     # the circuit, D2H of the final state, every step

@@ -33,7 +33,7 @@
 
 namespace qi {
 
-constexpr int kPolyThreads = 256, kPolyMaxH = 12, kPolyUnroll = 4;
+constexpr int kPolyThreads = 256, kPolyMaxH = 12, kPolyUnroll = 8;
 // device block layout (32-bit words)
 constexpr int kPolyA = 0, kPolyB = 64, kPolyT1 = 64 + 64 * 64, kPolyG0 = kPolyT1 + 2 * 1024;
 
@@ -82,7 +82,7 @@ bool phase_poly_add_table(PhasePoly &pp, int k, const int32_t *qubits, const std
 // Threads 2^m and iterations 2^h with m + h = n - 1 (amplitude pairs).
 int phase_poly_iter_bits(int n) {
     const int pairs = n - 1;
-    int m = std::min(pairs, 17);
+    int m = std::min(pairs, 19);
     int h = pairs - m;
     if (h > kPolyMaxH) h = kPolyMaxH;
     return h;
@@ -160,20 +160,31 @@ __global__ void __launch_bounds__(kPolyThreads) k_phase_poly(float4 *v, const ui
         for (int k = 0; k < kPolyMaxH; ++k)
             if (k < h) gam[k] += b[j * 64 + m + 1 + k];
     }
+    // cross terms of the low log2(kPolyUnroll) iteration bits, one value per unrolled slot
+    uint32_t low[kPolyUnroll];
+#pragma unroll
+    for (int u = 0; u < kPolyUnroll; ++u) {
+        low[u] = 0;
+#pragma unroll
+        for (int k = 0; (1 << k) < kPolyUnroll; ++k)
+            if (k < h && ((u >> k) & 1)) low[u] += gam[k];
+    }
     const uint32_t iters = 1u << h;
     for (uint32_t it0 = 0; it0 < iters; it0 += kPolyUnroll) {
         float4 x[kPolyUnroll];
 #pragma unroll
         for (int u = 0; u < kPolyUnroll; ++u)
             if (it0 + u < iters) x[u] = __ldcs(v + (((uint64_t)(it0 + u) << m) | tid));
+        // cross terms of the remaining iteration bits, once per group of kPolyUnroll
+        uint32_t base = F;
+#pragma unroll
+        for (int k = 0; k < kPolyMaxH; ++k)
+            if ((1 << k) >= kPolyUnroll && k < h && ((it0 >> k) & 1u)) base += gam[k];
 #pragma unroll
         for (int u = 0; u < kPolyUnroll; ++u) {
             const uint32_t it = it0 + u;
             if (it >= iters) break;
-            uint32_t f = F + __ldg(G0 + it);
-#pragma unroll
-            for (int k = 0; k < kPolyMaxH; ++k)
-                if (k < h && ((it >> k) & 1u)) f += gam[k];
+            const uint32_t f = base + low[u] + __ldg(G0 + it);
             const uint32_t f1 = f + P0 + __ldg(G1 + it);
             const float2 p0 = turn_phase(f, T1), p1 = turn_phase(f1, T1);
             float4 y;

@@ -197,6 +197,47 @@ def adjoint_leg(qi, workloads, stream, torch, np, n=26, layers=12):
             "rel_err_fp32_adjoint_vs_fd_subset": rel_fd32, "fd_subset": [int(x) for x in ids]}
 
 
+def trotter_leg(qi, workloads, stream, torch, np, rows=5, cols=6, steps=20, observe_every=10):
+    """First-order Trotter evolution on the 5x6 open lattice (30 qubits): anisotropic
+    Heisenberg (1.0 XX + 0.8 YY + 0.5 ZZ per bond, h_i Z_i), 177 terms, dt = 0.05, from a
+    seeded basis state.  The FP32 fused step (one plan per step, <H> every 10 steps) is
+    timed over `steps` steps; the FP64 step (one exp(-i c dt P) pass per term, the
+    reference's data flow) is timed over 2 steps, and <H> after 2 steps of both is compared."""
+    n = rows * cols
+    terms = workloads.lattice_xyz(rows, cols, seed=0)
+    basis = int(np.random.default_rng(0).integers(0, 1 << n))
+    out = {"workload": "5x6 lattice anisotropic Heisenberg, %d terms, dt 0.05, basis state %d" % (len(terms), basis),
+           "steps": steps}
+    s32 = qi.DeviceState(n, qi.F32)
+    s32.set_stream(stream.cuda_stream)
+    s32.set_basis(basis)
+    qi.trotter_evolve(s32, terms, 0.05, 2)   # warm-up (plan build, first launches)
+    e32_2 = qi.sumop_expectation(s32, terms).real
+    s32.set_basis(basis)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    e32 = qi.trotter_evolve(s32, terms, 0.05, steps, observable=terms, observe_every=observe_every)
+    t32 = time.perf_counter() - t0
+    s32.close()
+    s64 = qi.DeviceState(n, qi.F64)
+    s64.set_stream(stream.cuda_stream)
+    s64.set_basis(basis)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    qi.trotter_evolve(s64, terms, 0.05, 2)
+    t64_step = (time.perf_counter() - t0) / 2
+    e64_2 = qi.sumop_expectation(s64, terms).real
+    s64.close()
+    out.update({"fp32_fused_ms_per_step": t32 * 1e3 / steps, "fp64_per_term_ms_per_step": t64_step * 1e3,
+                "speedup_fp32_fused_vs_fp64_per_term": t64_step / (t32 / steps),
+                "term_exponentials_per_s_fp32": len(terms) * steps / t32,
+                "energies_fp32_every_%d" % observe_every: [complex(e).real for e in e32],
+                "energy_after_2_steps_fp32_fused": e32_2, "energy_after_2_steps_fp64_per_term": e64_2,
+                "energy_error_fp32_2_steps": abs(e32_2 - e64_2),
+                "note": "FP32 timed region includes the <H> evaluations (every %d steps)" % observe_every})
+    return out
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -412,6 +453,7 @@ def main():
                  "energy_error": abs(energy - energy64),
                  "gates_per_s_fused": len(gates) / (ms_per_step / 1e3)}
         extra["adjoint"] = adjoint_leg(qi, workloads, stream, torch, np)
+        extra["trotter"] = trotter_leg(qi, workloads, stream, torch, np)
     extra["expectation"] = expectation
 
     # end-to-end through the public API with host buffers: H2D of the initial state,

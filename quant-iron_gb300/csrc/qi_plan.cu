@@ -666,11 +666,21 @@ qi_status qi_trotter_evolve(qi_state *s, const qi_pauli_term *terms, int64_t n_t
         for (int64_t k = 0; k < n_terms; ++k) elems.push_back(pauli_exp_elem(terms[k], 0.0, -dt / 2.0, (int)k));
         for (int64_t k = n_terms - 1; k >= 0; --k) elems.push_back(pauli_exp_elem(terms[k], 0.0, -dt / 2.0, (int)k));
     }
+    // FP32: the step is one fused plan: narrow exponentials compose into dense
+    // blocks (FP64 composition) and runs of Z-type exponentials into phase
+    // polynomials.  With real coefficients every exponential is unitary, so the
+    // plan may use the tensor-core blocks and renormalise once per step; complex
+    // coefficients (a non-unitary step) keep the CUDA-core blocks and the norm.
+    // FP64: one memory-bound pass per exponential (FP64 arithmetic is scarce on
+    // this part, so dense FP64 blocks would be compute-bound).
+    bool unitary = true;
+    for (int64_t k = 0; k < n_terms; ++k) unitary = unitary && terms[k].coeff_im == 0.0;
     qi_plan plan;
     plan.n = s->n;
     plan.prec = s->prec;
-    plan.opts.fusion = QI_FUSION_NONE;
-    if (const char *f = std::getenv("QI_TROTTER_FUSION")) plan.opts.fusion = std::atoi(f);
+    plan.opts.fusion = s->prec == QI_F32 ? QI_FUSION_GREEDY : QI_FUSION_NONE;
+    plan.opts.use_tensor_cores = unitary ? 1 : 2;
+    plan.opts.renorm_every = unitary ? 0 : -1;
     plan.opts.max_block_qubits = 0;
     Status st = build_plan(&plan, elems);
     if (st.ok()) st = upload_plan(&plan);

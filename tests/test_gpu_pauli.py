@@ -81,6 +81,38 @@ def test_trotter_vs_oracle(qi, orc, prec, order):
     assert abs(energies[-1] - orc.sumop_expectation(want, n, terms)) < (1e-10 if prec == 0 else 1e-4)
 
 
+@pytest.mark.parametrize("prec", [0, 1], ids=["f64", "f32"])
+def test_trotter_fused_14q_vs_oracle(qi, orc, prec):
+    """2 x 7 lattice: the fused step has 5- and 6-qubit blocks (tensor cores for FP32,
+    renormalised per step) and phase polynomials for the Z-type exponentials."""
+    n = 14
+    terms = workloads.lattice_xyz(2, 7, seed=5)
+    init = workloads.basis_state(n, 0b10110010110101)
+    want = orc.trotter(init, n, terms, 0.05, 5, 1)
+    with qi.DeviceState(n, prec) as st:
+        st.upload(init)
+        qi.trotter_evolve(st, terms, 0.05, 5, order=1)
+        got = st.download()
+    assert np.max(np.abs(got - want)) < (1e-11 if prec == 0 else 2e-5)
+
+
+@pytest.mark.parametrize("prec", [0, 1], ids=["f64", "f32"])
+def test_trotter_complex_coefficients_keep_the_norm_change(qi, orc, prec):
+    """Complex coefficients make the step non-unitary (exp(-i c dt P) with Im c != 0):
+    no renormalisation, the norm changes exactly as in the oracle."""
+    n = 13
+    terms = workloads.lattice_xyz(1, 13, seed=7)
+    terms["im"][::5] = 0.3
+    init = workloads.plus_state(n)
+    want = orc.trotter(init, n, terms, 0.05, 4, 1)
+    with qi.DeviceState(n, prec) as st:
+        st.upload(init)
+        qi.trotter_evolve(st, terms, 0.05, 4, order=1)
+        got = st.download()
+    assert abs(np.vdot(want, want).real - 1.0) > 1e-3   # the reference step changes the norm
+    assert np.max(np.abs(got - want)) < (1e-11 if prec == 0 else 2e-5)
+
+
 def test_trotter_errors(qi):
     with qi.DeviceState(3, 0) as st:
         st.set_zero()

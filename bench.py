@@ -280,8 +280,9 @@ def run_reference(args):
 
 
 def profile_case_fused26():
-    """Small case for ncu (26 qubits FP32 = 512 MB, larger than L2): the first 8 ops of the
-    fused k<=6 plan of the 26-qubit random circuit, twice (k_fused_tc and k_diagk launches)."""
+    """Small case for ncu (26 qubits FP32 = 512 MB, larger than L2): the fused k<=6 plan of
+    the 26-qubit random circuit, twice (k_fused_tc, k_phase_poly, k_diagk launches), then one
+    <H> of the 26-qubit open-chain Heisenberg (k_xgroup_expect_f32, k_diag_expect_f32)."""
     import __graft_entry__ as ge
     qi = ge.load_package()
     from quant_iron_gb300 import workloads
@@ -293,7 +294,8 @@ def profile_case_fused26():
     for _ in range(2):
         plan.execute(st)
     st.synchronize()
-    print("profile case done, norm^2 = %.9f" % st.norm_sqr())
+    e = qi.sumop_expectation(st, workloads.heisenberg_open_chain(n)).real
+    print("profile case done, norm^2 = %.9f, <H> = %.9f" % (st.norm_sqr(), e))
 
 
 def main():

@@ -301,10 +301,17 @@ __device__ __forceinline__ void split_store(uint32_t taddr_hi, uint32_t taddr_lo
     tmem_st<N>(taddr_lo, v);
 }
 
-template <int K>
+// PAIR: a CTA takes tiles in pairs (2p, 2p+1), which differ in qubit L, so the row
+// runs of the two tiles are adjacent in memory; one bulk copy of 2 x 2^L amplitudes per
+// row run loads both.  The two shared buffers then hold the pair's row halves (top
+// target bit 0 / 1), read by converter slice 0 / 1, and are released after the pair's
+// second tile.  Used when the runs are short (1-2 KB), where the copy granularity bounds
+// the load rate.
+template <int K, bool PAIR>
 __global__ void __launch_bounds__(kTcThreads, 1) k_fused_tc(float2 *a, const float *blocks, TileGeom g, int *err_flag) {
     using C = TcCfg<K>;
     constexpr int R = C::R, NB = C::NBUF;
+    static_assert(!PAIR || NB == 2, "pair mode uses one buffer per converter slice");
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     float *sB = reinterpret_cast<float *>(smem_raw);   // 6 operand blocks: -Im, Re, Im (hi), then (lo)
     unsigned char *tiles = smem_raw + C::OFF_TILES;
@@ -336,7 +343,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_fused_tc(float2 *a, const flo
         }
         for (int j = 0; j < g.nhigh; ++j) {
             const uint32_t bit = ((uint32_t)tid >> (g.nlow_t + j)) & 1u;
-            x |= bit << (g.L + j);
+            // pair mode: the top high target selects the buffer; the others index runs of 2 x 2^L
+            if (!PAIR) x |= bit << (g.L + j);
+            else if (j < g.nhigh - 1) x |= bit << (g.L + 1 + j);
             go |= (uint64_t)bit << g.high_t[j];
         }
         rowx[tid] = x;
@@ -345,7 +354,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_fused_tc(float2 *a, const flo
     if (tid == 0) {
         for (int i = 0; i < NB; ++i) {
             mbar_init(raw_full + i, 1);
-            mbar_init(raw_empty + i, kConvWarps);
+            mbar_init(raw_empty + i, PAIR ? kConvWarps / 2 : kConvWarps);
         }
         for (int i = 0; i < 2; ++i) {
             mbar_init(a_full + i, kConvWarps);
@@ -363,7 +372,12 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_fused_tc(float2 *a, const flo
     tc_fence_after();
     const uint32_t tmem = *tmem_slot;
     // tile counts stay below 2^32 (2^(n-13) tiles for n <= 44)
-    const uint32_t ntiles = (uint32_t)g.ntiles, t0 = blockIdx.x, tstep = gridDim.x;
+    const uint32_t ntiles = (uint32_t)g.ntiles;
+    // iteration -> tile; pair mode takes 2p and 2p + 1 in consecutive iterations
+    auto tile_of = [&](int it) -> uint32_t {
+        return PAIR ? 2u * (blockIdx.x + (uint32_t)(it >> 1) * gridDim.x) + (uint32_t)(it & 1)
+                    : blockIdx.x + (uint32_t)it * gridDim.x;
+    };
     const bool pair_rows = !g.q0_is_col;   // qubit 0 is target 0: rows r, r+1 are adjacent amplitudes
 
     if (warp < kConvWarps) {
@@ -372,11 +386,13 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_fused_tc(float2 *a, const flo
         const uint32_t cx = tile_colx(g, (uint32_t)(quarter * 32 + lane));
         const uint32_t lane_base = (uint32_t)(quarter * 32) << 16;
         const int r0 = slice * C::CONV_ROWS;
-        int it = 0;
-        for (uint32_t t = t0; t < ntiles; t += tstep, ++it) {
-            const int b = it % NB;
-            if (!warp_wait_or_abort(raw_full + b, (uint32_t)(it / NB) & 1u, abort_flag, err_flag)) break;
-            const float2 *S = reinterpret_cast<const float2 *>(tiles + (size_t)b * C::TILE_BYTES);
+        for (int it = 0; tile_of(it) < ntiles; ++it) {
+            const int b = PAIR ? slice : it % NB;
+            const bool first = !PAIR || (it & 1) == 0;   // pair mode: the pair's 2nd tile reuses the buffer
+            const uint32_t ph = PAIR ? (uint32_t)(it >> 1) & 1u : (uint32_t)(it / NB) & 1u;
+            if (first && !warp_wait_or_abort(raw_full + b, ph, abort_flag, err_flag)) break;
+            const float2 *S = reinterpret_cast<const float2 *>(tiles + (size_t)b * C::TILE_BYTES) +
+                              (PAIR ? ((uint32_t)(it & 1) << g.L) : 0u);
             // real half -> A stage 0, once the products of the previous tile have read it;
             // the imaginary parts stay in registers for stage 1
             if (it > 0 && !warp_wait_or_abort(a_empty + 0, (uint32_t)(it - 1) & 1u, abort_flag, err_flag)) break;
@@ -406,7 +422,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_fused_tc(float2 *a, const flo
                                       re);
             }
             __syncwarp();
-            if (lane == 0) mbar_arrive(raw_empty + b);   // the buffer may take the next tile
+            if (lane == 0 && (!PAIR || (it & 1))) mbar_arrive(raw_empty + b);   // the buffer may take the next tile
             tmem_wait_st();
             tc_fence_before();
             __syncwarp();
@@ -429,8 +445,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_fused_tc(float2 *a, const flo
         const int quarter = warp & 3;
         const uint64_t cx = tile_colx(g, (uint32_t)(quarter * 32 + lane));
         const uint32_t lane_base = (uint32_t)(quarter * 32) << 16;
-        int it = 0;
-        for (uint32_t t = t0; t < ntiles; t += tstep, ++it) {
+        for (int it = 0; tile_of(it) < ntiles; ++it) {
+            const uint32_t t = tile_of(it);
             const int d = it & 1;
             if (!warp_wait_or_abort(d_full + d, (uint32_t)(it >> 1) & 1u, abort_flag, err_flag)) break;
             tc_fence_after();
@@ -464,22 +480,48 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_fused_tc(float2 *a, const flo
         // ------------------------------------------------ producer (one thread)
         if (lane == 0) {
             const uint32_t run_bytes = (uint32_t)sizeof(float2) << g.L;
-            const int nruns = 1 << g.nhigh;
-            int it = 0, issued = 0;
-            for (uint32_t t = t0; t < ntiles; t += tstep, ++it) {
-                const int b = it % NB;
-                if (it >= NB && !wait_or_abort(raw_empty + b, (uint32_t)(it / NB - 1) & 1u, abort_flag, err_flag))
-                    break;
-                mbar_arrive_expect_tx(raw_full + b, C::TILE_BYTES);
-                const uint64_t base = tile_base(g, t);
-                unsigned char *dst = tiles + (size_t)b * C::TILE_BYTES;
-                for (int h = 0; h < nruns; ++h)
-                    bulk_load(dst + (size_t)h * run_bytes, a + (base | grow[h << g.nlow_t]), run_bytes, raw_full + b);
-                issued = it + 1;
+            if (!PAIR) {
+                const int nruns = 1 << g.nhigh;
+                int issued = 0;
+                for (int it = 0; tile_of(it) < ntiles; ++it) {
+                    const int b = it % NB;
+                    if (it >= NB && !wait_or_abort(raw_empty + b, (uint32_t)(it / NB - 1) & 1u, abort_flag, err_flag))
+                        break;
+                    mbar_arrive_expect_tx(raw_full + b, C::TILE_BYTES);
+                    const uint64_t base = tile_base(g, tile_of(it));
+                    unsigned char *dst = tiles + (size_t)b * C::TILE_BYTES;
+                    for (int h = 0; h < nruns; ++h)
+                        bulk_load(dst + (size_t)h * run_bytes, a + (base | grow[h << g.nlow_t]), run_bytes, raw_full + b);
+                    issued = it + 1;
+                }
+                // copies still in flight (only after an abort) land before the CTA exits
+                for (int j = issued > NB ? issued - NB : 0; j < issued; ++j)
+                    if (!mbar_wait_bounded(raw_full + (j % NB), (uint32_t)(j / NB) & 1u)) atomicExch(err_flag, 2);
+            } else {
+                // buffer s <- the pair's rows with top target bit s: runs of 2 x 2^L amplitudes
+                const int half_runs = 1 << (g.nhigh - 1);
+                int issued[2] = {0, 0};
+                bool ok = true;
+                for (int ip = 0; ok && tile_of(2 * ip) < ntiles; ++ip) {
+                    const uint64_t base = tile_base(g, tile_of(2 * ip));
+                    for (int s = 0; s < 2; ++s) {
+                        if (ip >= 1 && !wait_or_abort(raw_empty + s, (uint32_t)(ip - 1) & 1u, abort_flag, err_flag)) {
+                            ok = false;
+                            break;
+                        }
+                        mbar_arrive_expect_tx(raw_full + s, C::TILE_BYTES);
+                        unsigned char *dst = tiles + (size_t)s * C::TILE_BYTES;
+                        for (int h = 0; h < half_runs; ++h)
+                            bulk_load(dst + (size_t)h * 2 * run_bytes,
+                                      a + (base | grow[(h | (s << (g.nhigh - 1))) << g.nlow_t]), 2 * run_bytes,
+                                      raw_full + s);
+                        issued[s] = ip + 1;
+                    }
+                }
+                for (int s = 0; s < 2; ++s)
+                    if (issued[s] > 0 && !mbar_wait_bounded(raw_full + s, (uint32_t)(issued[s] - 1) & 1u))
+                        atomicExch(err_flag, 2);
             }
-            // copies still in flight (only after an abort) land before the CTA exits
-            for (int j = issued > NB ? issued - NB : 0; j < issued; ++j)
-                if (!mbar_wait_bounded(raw_full + (j % NB), (uint32_t)(j / NB) & 1u)) atomicExch(err_flag, 2);
         }
         __syncwarp();
     } else {
@@ -489,9 +531,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_fused_tc(float2 *a, const flo
             // (>> 4 into the start-address field, which cannot carry: blocks stay below 256 KB).
             const uint64_t desc0 = smem_desc(smem_u32(sB), C::LBO, C::SBO);
             constexpr uint32_t idesc = tf32_idesc(128, 2 * R);
-            int it = 0;
             bool ok = true;
-            for (uint32_t t = t0; ok && t < ntiles; t += tstep, ++it) {
+            for (int it = 0; ok && tile_of(it) < ntiles; ++it) {
                 const int d = it & 1;
                 if (it >= 2 && !wait_or_abort(d_empty + d, (uint32_t)((it >> 1) - 1) & 1u, abort_flag, err_flag))
                     break;
@@ -566,23 +607,23 @@ void tc_blocks(int k, const double *U, std::vector<float> &out) {
     }
 }
 
-template <int K>
+template <int K, bool PAIR>
 static Status launch_tc_t(qi_state *s, const TileGeom &g, const void *d_tc) {
     using C = TcCfg<K>;
     static_assert(C::SMEM <= 232448, "shared memory per CTA");
     static bool attr_set = false;
     static int num_sms = 0;
     if (!attr_set) {
-        QI_CUDA(cudaFuncSetAttribute(k_fused_tc<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::SMEM));
+        QI_CUDA(cudaFuncSetAttribute(k_fused_tc<K, PAIR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::SMEM));
         int dev = 0;
         QI_CUDA(cudaGetDevice(&dev));
         QI_CUDA(cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, dev));
         attr_set = true;
     }
-    uint64_t grid = g.ntiles;   // one persistent CTA per SM
+    uint64_t grid = PAIR ? g.ntiles / 2 : g.ntiles;   // one persistent CTA per SM
     if (grid > (uint64_t)num_sms) grid = (uint64_t)num_sms;
-    k_fused_tc<K><<<(unsigned)grid, kTcThreads, C::SMEM, s->stream>>>((float2 *)s->amps, (const float *)d_tc, g,
-                                                                      s->d_flag);
+    k_fused_tc<K, PAIR><<<(unsigned)grid, kTcThreads, C::SMEM, s->stream>>>((float2 *)s->amps, (const float *)d_tc,
+                                                                            g, s->d_flag);
     count_launch();
     return check_launch("k_fused_tc");
 }
@@ -594,7 +635,12 @@ Status launch_fused_tc(qi_state *s, int k, const int32_t *targets, const void *d
     const TileGeom g = make_tile_geom(n, k, targets, 7);
     if (g.nfree != n - k - 7) return err(QI_ERR_UNKNOWN, g.nfree, n - k - 7, "tile decomposition");
     if (((uintptr_t)d_tc & 15) != 0) return err(QI_ERR_UNKNOWN, -1, -1, "operand blocks must be 16-byte aligned");
-    return k == 6 ? launch_tc_t<6>(s, g, d_tc) : launch_tc_t<5>(s, g, d_tc);
+    // Tile pairs when a tile's rows are 1 KB runs (all targets at qubit 7 or above): tiles 2p,
+    // 2p + 1 differ in qubit L = 7, so each pair of runs is one 2 KB copy.  (Measured: 1 KB runs
+    // gain ~8 %; with 2 KB runs the pair's longer buffer occupancy costs more than it saves.)
+    const bool pair = k == 6 && g.nhigh >= 1 && g.nfree >= 1 && g.L == 7 && g.L < n;
+    if (k == 5) return launch_tc_t<5, false>(s, g, d_tc);
+    return pair ? launch_tc_t<6, true>(s, g, d_tc) : launch_tc_t<6, false>(s, g, d_tc);
 }
 
 }  // namespace qi

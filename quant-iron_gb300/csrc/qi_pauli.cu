@@ -16,6 +16,7 @@
 #include <algorithm>
 #include <cmath>
 #include <map>
+#include <type_traits>
 
 namespace qi {
 
@@ -49,6 +50,29 @@ __global__ void __launch_bounds__(256) k_pauli_exp_diag(typename Cx<T>::V2 *a, E
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < p.nwork; i += stride) {
         typename X::V2 v = a[i];
         a[i] = X::mul((__popcll(i & p.zmask) & 1) ? minus : plus, v);
+    }
+}
+
+// FP64 pair case for exp(-i theta P) with a real coefficient: c = cos(theta) is
+// real and s is real (SIMAG = false) or imaginary (SIMAG = true), so each output
+// costs 4 FP64 operations instead of 8 (FP64 arithmetic bounds this kernel here).
+template <bool SIMAG>
+__global__ void __launch_bounds__(256) k_pauli_exp_pair_real64(double2 *a, ExpParams p) {
+    const double c = p.cre, s = SIMAG ? p.sim : p.sre;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    const uint64_t lo_mask = p.hbit - 1;
+    for (uint64_t w = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; w < p.nwork; w += stride) {
+        const uint64_t i = ((w & ~lo_mask) << 1) | (w & lo_mask);
+        const uint64_t j = i ^ p.xmask;
+        const double2 x = a[i], y = a[j];
+        const double si = (__popcll(i & p.zmask) & 1) ? -s : s, sj = (__popcll(j & p.zmask) & 1) ? -s : s;
+        if (SIMAG) {   // c x + i s y
+            a[i] = make_double2(::fma(-si, y.y, c * x.x), ::fma(si, y.x, c * x.y));
+            a[j] = make_double2(::fma(-sj, x.y, c * y.x), ::fma(sj, x.x, c * y.y));
+        } else {       // c x + s y
+            a[i] = make_double2(::fma(si, y.x, c * x.x), ::fma(si, y.y, c * x.y));
+            a[j] = make_double2(::fma(sj, x.x, c * y.x), ::fma(sj, x.y, c * y.y));
+        }
     }
 }
 
@@ -136,6 +160,10 @@ Status launch_pauli_exp(qi_state *s, uint64_t xmask, uint64_t zmask, double cre,
     if (f32) {
         if (vec) k_pauli_exp_pair<float, true><<<g, 256, 0, s->stream>>>((float2 *)s->amps, p);
         else k_pauli_exp_pair<float, false><<<g, 256, 0, s->stream>>>((float2 *)s->amps, p);
+    } else if (p.cim == 0.0 && p.sre == 0.0) {
+        k_pauli_exp_pair_real64<true><<<g, 256, 0, s->stream>>>((double2 *)s->amps, p);
+    } else if (p.cim == 0.0 && p.sim == 0.0) {
+        k_pauli_exp_pair_real64<false><<<g, 256, 0, s->stream>>>((double2 *)s->amps, p);
     } else {
         k_pauli_exp_pair<double, false><<<g, 256, 0, s->stream>>>((double2 *)s->amps, p);
     }
@@ -445,10 +473,16 @@ __global__ void __launch_bounds__(256) k_sumop_apply(typename Cx<T>::V2 *o, cons
                                                      const GroupHdr *groups, int ngroups, const GroupTerm *terms,
                                                      int nterms) {
     using X = Cx<T>;
-    extern __shared__ unsigned char smem_raw[];
-    GroupTerm *sterm = reinterpret_cast<GroupTerm *>(smem_raw);
+    // FP32 states keep the coefficients in shared memory already rounded to FP32
+    // (converting FP64 per element would run on the scarce FP64 pipe)
+    using Term = typename std::conditional<sizeof(T) == 4, TermF, GroupTerm>::type;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    Term *sterm = reinterpret_cast<Term *>(smem_raw);
     GroupHdr *shdr = reinterpret_cast<GroupHdr *>(sterm + nterms);
-    for (int k = threadIdx.x; k < nterms; k += blockDim.x) sterm[k] = terms[k];
+    for (int k = threadIdx.x; k < nterms; k += blockDim.x) {
+        if constexpr (sizeof(T) == 4) sterm[k] = term_f32(terms[k]);
+        else sterm[k] = terms[k];
+    }
     for (int k = threadIdx.x; k < ngroups; k += blockDim.x) shdr[k] = groups[k];
     __syncthreads();
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
@@ -456,7 +490,9 @@ __global__ void __launch_bounds__(256) k_sumop_apply(typename Cx<T>::V2 *o, cons
         typename X::V2 acc = X::make(0, 0);
         for (int g = 0; g < ngroups; ++g) {
             const GroupHdr h = shdr[g];
-            typename X::V2 f = group_factor<T>(sterm + h.first, h.count, i);
+            typename X::V2 f;
+            if constexpr (sizeof(T) == 4) f = factor_f32_n(sterm + h.first, h.count, i);
+            else f = group_factor<T>(sterm + h.first, h.count, i);
             acc = X::fma(f, in[i ^ h.xmask], acc);
         }
         o[i] = acc;

@@ -63,6 +63,24 @@ __global__ void k_convert(typename Cx<TO>::V2 *o, const typename Cx<TI>::V2 *in,
     }
 }
 
+// The same conversion for a buffer on the other side of the CPU-GPU link (mapped,
+// page-locked host memory): four independent 16-byte accesses in flight per
+// thread to cover the link's latency.
+template <typename TO, typename TI>
+__global__ void __launch_bounds__(256) k_convert_link(typename Cx<TO>::V2 *o, const typename Cx<TI>::V2 *in,
+                                                      uint64_t n) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i0 = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i0 < n; i0 += 4 * stride) {
+        typename Cx<TI>::V2 v[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+            if (i0 + u * stride < n) v[u] = in[i0 + u * stride];
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+            if (i0 + u * stride < n) o[i0 + u * stride] = Cx<TO>::make((TO)v[u].x, (TO)v[u].y);
+    }
+}
+
 template <typename T>
 __global__ void k_scale(typename Cx<T>::V2 *a, uint64_t dim, T re, T im) {
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < dim; i += (uint64_t)gridDim.x * blockDim.x) {
@@ -432,6 +450,18 @@ qi_status qi_state_synchronize(qi_state *s) {
 // Chunked transfer through a device staging buffer with on-device conversion.
 static constexpr uint64_t kChunkAmps = 1ull << 22;   // 4 Mi amplitudes = 64 MiB of f64 pairs
 
+// Device-side address of a page-locked, mapped, 16-byte aligned host buffer (the GPU
+// reads and writes it directly over the CPU-GPU link), or nullptr otherwise.
+static void *mapped_host_ptr(const void *p) {
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return nullptr;
+    }
+    if (at.type != cudaMemoryTypeHost || !at.devicePointer || ((uintptr_t)at.devicePointer & 15) != 0) return nullptr;
+    return at.devicePointer;
+}
+
 qi_status qi_state_upload(qi_state *s, const double *amps, uint64_t num_amps) {
     QI_GUARD(s);
     if (!amps) return publish(err(QI_ERR_NULL_ARGUMENT));
@@ -440,6 +470,12 @@ qi_status qi_state_upload(qi_state *s, const double *amps, uint64_t num_amps) {
         cudaError_t e = cudaMemcpyAsync(s->amps, amps, s->bytes(), cudaMemcpyHostToDevice, s->stream);
         if (e != cudaSuccess) return publish(cuda_status(e, "upload"));
         return publish(ok_status());
+    }
+    if (const void *dp = mapped_host_ptr(amps)) {   // pinned: one pass reads the host buffer and converts
+        k_convert_link<float, double><<<grid_for(num_amps), 256, 0, s->stream>>>((float2 *)s->amps,
+                                                                                 (const double2 *)dp, num_amps);
+        count_launch();
+        return publish(check_launch("k_convert_link"));
     }
     const uint64_t chunk = num_amps < kChunkAmps ? num_amps : kChunkAmps;
     Status st = ensure_staging(s, 2 * chunk * 16);
@@ -462,6 +498,16 @@ qi_status qi_state_download(qi_state *s, double *amps, uint64_t num_amps) {
     if (s->prec == QI_F64) {
         cudaError_t e = cudaMemcpyAsync(amps, s->amps, s->bytes(), cudaMemcpyDeviceToHost, s->stream);
         if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+        if (e != cudaSuccess) return publish(cuda_status(e, "download"));
+        return publish(ok_status());
+    }
+    if (void *dp = mapped_host_ptr(amps)) {   // pinned: one pass converts and writes the host buffer
+        k_convert_link<double, float><<<grid_for(num_amps), 256, 0, s->stream>>>((double2 *)dp,
+                                                                                 (const float2 *)s->amps, num_amps);
+        count_launch();
+        Status st = check_launch("k_convert_link");
+        if (!st.ok()) return publish(st);
+        cudaError_t e = cudaStreamSynchronize(s->stream);
         if (e != cudaSuccess) return publish(cuda_status(e, "download"));
         return publish(ok_status());
     }

@@ -55,6 +55,14 @@ class DeviceState:
             lib.qi_state_destroy(self.h)
             self.h = ctypes.c_void_p()
 
+    def release(self):
+        """Hand the handle to a new owner: returns a DeviceState owning it and leaves this
+        object empty (so a `with` block ending afterwards frees nothing)."""
+        other = DeviceState.__new__(DeviceState)
+        other.h, other.n, other.precision = self.h, self.n, self.precision
+        self.h = ctypes.c_void_p()
+        return other
+
     def __del__(self):
         try:
             self.close()

@@ -3,18 +3,21 @@
 Same names, argument meaning and error behaviour as the Rust crate, so that
 code written against `quant_iron` reads the same here:
 
-  State (state.rs)              host-canonical `state_vector` like the Rust pub
-                                field; gate methods return new States
+  State (state.rs)              `state_vector` like the Rust pub field; gate
+                                methods return new States; measure / measure_n
+  MeasurementBasis, MeasurementResult (measurement.rs)
   Hadamard, Pauli, CNOT, ... (operator.rs)   Operator.apply(state, targets, controls)
   PauliString, SumOp (pauli_string.rs)
   Gate, Circuit (gate.rs, circuit.rs)
   first/second_order_trotter_step, trotter_evolve_state (time_evolution.rs)
 
-Every operation runs on the GPU: single operations upload, run one kernel and
-download (the reference's execute_on_gpu round trip, operator.rs:24-148);
-Circuit.execute, SumOp.expectation_value and the Trotter functions upload once
-and run all their passes on the resident state.  Errors raise
-QuantIronError whose `.variant` is the name of the Rust Error variant.
+Every operation runs on the GPU.  A State lives on the device once it has been
+used there: an operation copies it device to device, runs its kernels and
+returns a new State that owns the result, so chains (`st.h(0).cnot(0, 1)...`,
+`*_multi`, Circuit.execute, Trotter steps) never round-trip through the host.
+`state_vector` is downloaded on first read (and cached); assigning it replaces
+the device copy.  Errors raise QuantIronError whose `.variant` is the name of
+the Rust Error variant.
 """
 import math
 
@@ -24,6 +27,7 @@ from . import _abi
 from . import DeviceState, Plan, sumop_expectation as _expect, sumop_apply as _sumop_apply
 from . import pauli_apply as _pauli_apply, pauli_apply_normalised as _pauli_norm
 from . import pauli_apply_exp_factor as _pauli_exp_factor, trotter_evolve as _trotter
+from . import measure as _measure, measure_n as _measure_n
 from ._abi import F32, F64, FUSION_GREEDY, FUSION_NONE, GATE_DTYPE, TERM_DTYPE, QuantIronError, check, lib
 from .workloads import GateList, qft as _qft
 
@@ -39,11 +43,37 @@ def _err(variant_code, a=-1, b=-1):
 
 # --------------------------------------------------------------------- State
 class State:
-    """`State { state_vector, num_qubits }` (state.rs:74-81)."""
+    """`State { state_vector, num_qubits }` (state.rs:74-81).  Holds a host copy, a
+    device copy, or both; `state_vector` reads download once and cache."""
 
-    def __init__(self, state_vector, num_qubits):
-        self.state_vector = np.ascontiguousarray(state_vector, dtype=np.complex128)
+    def __init__(self, state_vector, num_qubits, _dev=None):
         self.num_qubits = int(num_qubits)
+        self._host = None if state_vector is None else np.ascontiguousarray(state_vector, dtype=np.complex128)
+        self._dev = _dev
+
+    @property
+    def state_vector(self):
+        if self._host is None:
+            self._host = self._dev.download()
+        return self._host
+
+    @state_vector.setter
+    def state_vector(self, v):
+        self._host = np.ascontiguousarray(v, dtype=np.complex128)
+        self._dev = None
+
+    @staticmethod
+    def _take(d, n):
+        """A State owning the device state `d` (no download)."""
+        return State(None, n, _dev=d.release())
+
+    def _resident(self):
+        """The device copy (uploaded on first use); read-only for callers."""
+        if self._dev is None:
+            d = DeviceState(self.num_qubits, PRECISION)
+            d.upload(self._host)
+            self._dev = d
+        return self._dev
 
     # constructors (state.rs:99-373)
     @staticmethod
@@ -56,8 +86,7 @@ class State:
             raise _err(-3, int(math.floor(math.log2(ln))))
         n = ln.bit_length() - 1
         st = State(v, n)
-        with st._device() as d:
-            d.check_normalised()
+        st._resident().check_normalised()
         return st
 
     @staticmethod
@@ -66,7 +95,7 @@ class State:
             raise _err(-3, 0)
         with DeviceState(n, PRECISION) as d:
             fill(d)
-            return State(d.download(), n)
+            return State._take(d, n)
 
     @staticmethod
     def new_zero(n):
@@ -94,12 +123,16 @@ class State:
         return self.num_qubits
 
     def _device(self):
+        """A scratch device copy the caller may modify (device to device)."""
         d = DeviceState(self.num_qubits, PRECISION)
-        d.upload(self.state_vector)
+        d.copy_from(self._resident())
         return d
 
     def clone(self):
-        return State(self.state_vector.copy(), self.num_qubits)
+        if self._dev is None:
+            return State(self._host.copy(), self.num_qubits)
+        with self._device() as d:
+            return State._take(d, self.num_qubits)
 
     # PartialEq: per-component |diff| < f32::EPSILON (state.rs:2348-2372)
     def __eq__(self, other):
@@ -115,27 +148,26 @@ class State:
         return self.num_qubits == other.num_qubits and abs(abs(self.inner_product(other)) - 1.0) < F32_EPS
 
     def probability(self, n):
-        if n >= self.state_vector.size:
-            raise _err(-4, n, self.num_qubits)
-        return abs(self.state_vector[n]) ** 2
+        return abs(self.amplitude(n)) ** 2
 
     def amplitude(self, n):
-        if n >= self.state_vector.size:
+        if n >= (1 << self.num_qubits):
             raise _err(-4, n, self.num_qubits)
-        return self.state_vector[n]
+        if self._host is not None:
+            return self._host[n]
+        return self._dev.amplitude(n)   # one device read, no download
 
     def inner_product(self, other):   # state.rs:890-917
         if self.num_qubits == 0 or other.num_qubits == 0:
             raise _err(-3, 0)
-        if self.state_vector.size != other.state_vector.size:
+        if self.num_qubits != other.num_qubits:
             raise _err(-3, self.num_qubits)
-        with self._device() as a, other._device() as b:
-            return a.inner_product(b)
+        return self._resident().inner_product(other._resident())
 
     def normalise(self):   # state.rs:924-945
         with self._device() as d:
             d.normalise()
-            return State(d.download(), self.num_qubits)
+            return State._take(d, self.num_qubits)
 
     def fs_fidelity(self, other):
         return abs(self.normalise().inner_product(other.normalise())) ** 2
@@ -148,28 +180,29 @@ class State:
             raise _err(-3, 0)
         from . import tensor_product as _tp
         n = self.num_qubits + other.num_qubits
-        with self._device() as a, other._device() as b, DeviceState(n, PRECISION) as o:
-            _tp(o, a, b)
-            out = State(o.download(), n)
-        return State.new(out.state_vector)
+        with DeviceState(n, PRECISION) as o:
+            _tp(o, self._resident(), other._resident())
+            out = State._take(o, n)
+        out._resident().check_normalised()   # State::new's check
+        return out
 
     # arithmetic (state.rs:2687-2862)
     def __mul__(self, c):
         with self._device() as d:
             d.scale(complex(c))
-            return State(d.download(), self.num_qubits)
+            return State._take(d, self.num_qubits)
 
     __rmul__ = __mul__
 
     def __add__(self, other):
-        with self._device() as y, other._device() as x:
-            y.axpy(1.0, x)
-            return State(y.download(), self.num_qubits)
+        with self._device() as y:
+            y.axpy(1.0, other._resident())
+            return State._take(y, self.num_qubits)
 
     def __sub__(self, other):
-        with self._device() as y, other._device() as x:
-            y.axpy(-1.0, x)
-            return State(y.download(), self.num_qubits)
+        with self._device() as y:
+            y.axpy(-1.0, other._resident())
+            return State._take(y, self.num_qubits)
 
     # operate (state.rs:970-1002)
     def operate(self, op, target_qubits, control_qubits=()):
@@ -230,12 +263,93 @@ class State:
     def cunitary_multi(self, ts, cs, m): return self._multi(Unitary2.new(m), ts, cs)
     def ry_phase(self, i, th, ph): return Unitary2.from_ry_phase(th, ph).apply(self, [i], [])
     def ry_phase_dag(self, i, th, ph): return Unitary2.from_ry_phase_dagger(th, ph).apply(self, [i], [])
+    # measurement (state.rs:525-784)
+    def measure(self, basis=None, measured_qubits=(), seed=0):
+        """One draw (splitmix64(seed)) in `basis`; an empty `measured_qubits` measures all
+        qubits.  The State itself is unchanged; `new_state` of the result is collapsed."""
+        b, u = _basis_args(basis)
+        qs = [int(q) for q in measured_qubits] or list(range(self.num_qubits))
+        with self._device() as d:
+            o = _measure(d, qs, basis=b, custom=u, seed=seed)
+            new = State._take(d, self.num_qubits)
+        return MeasurementResult(basis or MeasurementBasis.Computational, qs, _bits(o, len(qs)), new)
+
+    def measure_n(self, basis, measured_qubits, n, seed=0):
+        """`n` draws (shot j uses splitmix64(seed + j)) from the same distribution.  Each
+        result's `new_state` is collapsed on first read: measuring a copy with seed + j
+        draws the same outcome."""
+        if n == 0:
+            raise _err(-1, 0)
+        b, u = _basis_args(basis)
+        qs = [int(q) for q in measured_qubits] or list(range(self.num_qubits))
+        if b == "Computational":
+            outs = _measure_n(self._resident(), n, qs, seed=seed)
+        else:   # the basis change and its undo round the amplitudes: use a scratch copy
+            with self._device() as d:
+                outs = _measure_n(d, n, qs, basis=b, custom=u, seed=seed)
+        label = basis or MeasurementBasis.Computational
+        return [MeasurementResult(label, qs, _bits(int(o), len(qs)),
+                                  _collapse=lambda j=j: self.measure(basis, qs, seed + j).new_state)
+                for j, o in enumerate(outs)]
+
     def cnot(self, control, target): return CNOT().apply(self, [target], [control])   # state.rs:2230-2232
     def swap(self, q1, q2): return SWAP().apply(self, [q1, q2], [])
     def cswap(self, t1, t2, cs): return SWAP().apply(self, [t1, t2], list(cs))
     def toffoli(self, c1, c2, t): return Toffoli().apply(self, [t], [c1, c2])
     def matchgate(self, t, th, p1, p2): return Matchgate(th, p1, p2).apply(self, [t], [])
     def cmatchgate(self, t, th, p1, p2, cs): return Matchgate(th, p1, p2).apply(self, [t], list(cs))
+
+
+# --------------------------------------------------------------- measurement
+class MeasurementBasis:
+    """`enum MeasurementBasis` (measurement.rs:76-86): Computational, X, Y, or
+    Custom(U) for a 2x2 unitary U."""
+    Computational = "Computational"
+    X = "X"
+    Y = "Y"
+
+    @staticmethod
+    def Custom(u):
+        return ("Custom", np.asarray(u, dtype=np.complex128).reshape(2, 2))
+
+
+def _basis_args(basis):
+    if basis is None:
+        return "Computational", None
+    if isinstance(basis, tuple):
+        return basis[0], basis[1]
+    return basis, None
+
+
+def _bits(o, m):
+    return [(o >> k) & 1 for k in range(m)]
+
+
+class MeasurementResult:
+    """`MeasurementResult { basis, indices, outcomes, new_state }` (measurement.rs:13-25);
+    outcomes[k] is the bit drawn for qubit indices[k]."""
+
+    def __init__(self, basis, indices, outcomes, new_state=None, _collapse=None):
+        self.basis, self.indices, self.outcomes = basis, list(indices), list(outcomes)
+        self._new, self._collapse = new_state, _collapse
+
+    @property
+    def new_state(self):
+        if self._new is None:
+            self._new = self._collapse()
+        return self._new
+
+    def get_basis(self):
+        return self.basis
+
+    def get_indices(self):
+        return self.indices
+
+    def get_outcomes(self):
+        return self.outcomes
+
+    def get_new_state(self):
+        return self.new_state
 
 
 # ----------------------------------------------------------------- operators
@@ -259,7 +373,7 @@ class Operator:
         row = self.gate_row(target_qubits, control_qubits)
         with state._device() as d:
             d.apply_gate(row)
-            return State(d.download(), state.num_qubits)
+            return State._take(d, state.num_qubits)
 
 
 def _op(name, kind, base=1):
@@ -388,19 +502,19 @@ class PauliString:
         return sorted(self.ops)
 
     def apply(self, state):
-        with state._device() as d, DeviceState(state.num_qubits, PRECISION) as o:
-            _pauli_apply(o, d, self.row())
-            return State(o.download(), state.num_qubits)
+        with DeviceState(state.num_qubits, PRECISION) as o:
+            _pauli_apply(o, state._resident(), self.row())
+            return State._take(o, state.num_qubits)
 
     def apply_normalised(self, state):
         with state._device() as d:
             _pauli_norm(d, self.row())
-            return State(d.download(), state.num_qubits)
+            return State._take(d, state.num_qubits)
 
     def apply_exp_factor(self, state, factor):
         with state._device() as d:
             _pauli_exp_factor(d, self.row(), factor)
-            return State(d.download(), state.num_qubits)
+            return State._take(d, state.num_qubits)
 
     def apply_exp(self, state):
         return self.apply_exp_factor(state, 1.0)
@@ -442,13 +556,12 @@ class SumOp:
         return a
 
     def apply(self, state):
-        with state._device() as d, DeviceState(state.num_qubits, PRECISION) as o:
-            _sumop_apply(o, d, self.rows())
-            return State(o.download(), state.num_qubits)
+        with DeviceState(state.num_qubits, PRECISION) as o:
+            _sumop_apply(o, state._resident(), self.rows())
+            return State._take(o, state.num_qubits)
 
     def expectation_value(self, state):
-        with state._device() as d:
-            return _expect(d, self.rows())
+        return _expect(state._resident(), self.rows())
 
 
 # -------------------------------------------------------------- gates/circuit
@@ -497,7 +610,7 @@ class Circuit:
         plan = Plan(self.num_qubits, PRECISION, self.gate_array(), fusion=FUSION)
         with initial_state._device() as d:
             plan.execute(d)
-            return State(d.download(), self.num_qubits)
+            return State._take(d, self.num_qubits)
 
     def trace_execution(self, initial_state):   # circuit.rs:188-202
         if initial_state.num_qubits != self.num_qubits:
@@ -522,7 +635,7 @@ def _trotter_call(hamiltonian, state, dt, steps, order):
         raise _err(-3, 0)
     with state._device() as d:
         _trotter(d, hamiltonian.rows(), dt, steps, order)
-        return State(d.download(), state.num_qubits)
+        return State._take(d, state.num_qubits)
 
 
 def first_order_trotter_step(hamiltonian, state, dt):

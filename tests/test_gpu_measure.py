@@ -143,3 +143,33 @@ def test_measure_24q_fp32_probabilities(qi):
         o64, p64 = qi.measure(s64, qubits, seed=5, return_probs=True)
     assert abs(p32.sum() - 1.0) < 1e-9
     assert np.max(np.abs(p32 - p64)) < 1e-6
+
+
+def test_mirror_state_measure(qi, orc):
+    """quant_iron.State.measure / measure_n: the crate's call shapes, outcomes equal the
+    oracle's for the same draw, and the measured State itself is unchanged."""
+    from quant_iron_gb300 import quant_iron as q
+    n, qubits = 8, [6, 1, 3]
+    init = rand_state(n, 41)
+    st = q.State.new(init)
+    for seed in range(4):
+        res = st.measure(q.MeasurementBasis.Computational, qubits, seed=seed)
+        want_o, want_state, _ = orc.measure(init, n, qubits, qi.splitmix_uniform(seed))
+        assert res.indices == qubits and res.basis == "Computational"
+        assert res.outcomes == [(want_o >> k) & 1 for k in range(3)]
+        assert np.max(np.abs(res.new_state.state_vector - want_state)) < 1e-12
+    assert np.array_equal(st.state_vector, init)
+    every = st.measure(q.MeasurementBasis.Computational, [], seed=3)
+    assert every.indices == list(range(n)) and len(every.outcomes) == n
+    shots = st.measure_n(q.MeasurementBasis.X, [2, 5], 6, seed=9)
+    for j, r in enumerate(shots):
+        one = st.measure(q.MeasurementBasis.X, [2, 5], seed=9 + j)
+        assert r.outcomes == one.outcomes and r.new_state == one.new_state
+    custom = q.MeasurementBasis.Custom([[0, 1], [1, 0]])
+    assert len(st.measure_n(custom, [0], 2)) == 2
+    with pytest.raises(qi.QuantIronError) as ei:
+        st.measure_n(q.MeasurementBasis.Computational, [0], 0)
+    assert ei.value.variant == "InvalidNumberOfMeasurements"
+    with pytest.raises(qi.QuantIronError) as ei:
+        st.measure(q.MeasurementBasis.Computational, [n])
+    assert ei.value.variant == "InvalidQubitIndex"

@@ -152,3 +152,15 @@ def test_mirror_api_reads_like_reference(qi):
     circ = q.qft_circuit([0, 1, 2], 3)
     out = circ.execute(q.State.new_zero(3))
     assert out == q.State.new_plus(3)
+
+
+def test_mirror_chain_stays_on_device(qi):
+    """A gate chain in the mirror downloads nothing until `state_vector` is read."""
+    from quant_iron_gb300 import quant_iron as q
+    st = q.State.new_zero(12).h_multi(range(12)).cnot(0, 5).rz(3, 0.4).swap(2, 9)
+    assert st._host is None and st._dev is not None
+    assert abs(st.probability(0) - 1.0 / 4096) < 1e-12 and st._host is None
+    v = st.state_vector
+    assert st._host is not None and abs(np.vdot(v, v) - 1.0) < 1e-12
+    st.state_vector = ka.zero(12)
+    assert st._dev is None and st.h(0).x(0).probability(1) == pytest.approx(0.5)

@@ -263,6 +263,9 @@ qi_status qi_trotter_evolve(qi_state *s, const qi_pauli_term *terms, int64_t n_t
 #define QI_FUSION_NONE    0  /* one kernel per gate (the plain per-gate method) */
 #define QI_FUSION_GREEDY  1  /* greedy fixed-k fuser, k = max_block_qubits */
 #define QI_FUSION_LEARNED 2  /* partitions scored by the learned cost model (greedy fallback) */
+#define QI_FUSION_PAULI_GROUPS 3  /* one kernel per gate, except that each run of Pauli exponentials
+                                     (Gate::PauliTimeEvolution) whose X-masks lie in {0, X} is one
+                                     pass (FP64 Trotter steps use this) */
 
 typedef struct qi_exec_options {
     int32_t fusion;            /* QI_FUSION_* */
@@ -367,15 +370,19 @@ qi_status qi_costmodel_set_params(const float *in, int64_t count, int32_t traine
 typedef struct qi_plan_op_info {
     int32_t  kind;          /* 1 one-target gate, 2 SWAP, 3 two-target gate, 4 fused dense block,
                                5 Pauli exponential, 6 Pauli string + normalise, 7 diagonal block,
-                               8 renormalisation, 9 phase polynomial (a run of diagonal blocks) */
-    int32_t  k;             /* number of targets (kind 9: number of diagonal blocks in the run) */
+                               8 renormalisation, 9 phase polynomial (a run of diagonal blocks),
+                               10 grouped Pauli exponentials (a run with X-masks in {0, X}) */
+    int32_t  k;             /* number of targets (kind 9: number of diagonal blocks in the run;
+                               kind 10: number of exponentials in the run) */
     int32_t  targets[6];    /* sorted ascending for kinds 3, 4, 7 */
     int32_t  tensor_cores;  /* kind 4: 1 if the block runs on the tcgen05 tensor-core kernel */
     int32_t  reserved;
     uint64_t control_mask;
-    uint64_t xmask, zmask;  /* kinds 5 and 6; kind 9: zmask = the qubits the run touches */
+    uint64_t xmask, zmask;  /* kinds 5 and 6; kind 9: zmask = the qubits the run touches;
+                               kind 10: xmask = X, zmask = OR of the parity basis masks */
     int64_t  n_matrix;      /* complex entries of the op's matrix: 4 (kind 1), 16 (kind 3), 4^k (kind 4),
-                               2^k (kind 7: the diagonal), 2 (kind 5: cosh(alpha), sinh(alpha)), else 0 */
+                               2^k (kind 7: the diagonal), 2 (kind 5: cosh(alpha), sinh(alpha)),
+                               kind 10: the tables (see qi_plan_op_pauli_group), else 0 */
 } qi_plan_op_info;
 qi_status qi_plan_num_ops(const qi_plan *p, int64_t *out);
 qi_status qi_plan_op_get(const qi_plan *p, int64_t i, qi_plan_op_info *info, double *matrix_out, int64_t capacity);
@@ -383,6 +390,13 @@ qi_status qi_plan_op_get(const qi_plan *p, int64_t i, qi_plan_op_info *info, dou
  * applied as exp(2 pi i f / 2^64) (coefficients in units of 2^-64 turns; a: n entries,
  * b: n*n entries, zero for q >= r).  Introspection aid; no reference counterpart. */
 qi_status qi_plan_op_phase_poly(const qi_plan *p, int64_t i, uint64_t *c0, uint64_t *a, uint64_t *b);
+/* Kind 10 ops: *n_tables tables (<= 4); table t is indexed by the parities
+ * beta_j = popcount(i & basis[8 t + j]) & 1, j < rank[t] (index bit j = beta_j),
+ * where i is the amplitude index (xmask == 0; the op multiplies amplitude i by the
+ * product of its tables' entries) or the pair member with the highest bit of
+ * xmask clear (one table of 2^rank[0] row-major 2x2 matrices acting on
+ * (psi_i, psi_{i ^ xmask})).  rank: 4 entries, basis: 32.  Introspection aid. */
+qi_status qi_plan_op_pauli_group(const qi_plan *p, int64_t i, int32_t *n_tables, int32_t *rank, uint64_t *basis);
 /* Execute the plan once with a CUDA event pair around every operation, on the
  * state's stream, and write each operation's device time in milliseconds to
  * ms_out (qi_plan_num_ops entries).  Measurement aid; no reference counterpart. */

@@ -16,11 +16,12 @@ import ctypes
 import numpy as np
 
 from . import _abi
-from ._abi import (F32, F64, FUSION_GREEDY, FUSION_LEARNED, FUSION_NONE, GATE_DTYPE, TERM_DTYPE, QuantIronError,
-                   check, lib)
+from ._abi import (F32, F64, FUSION_GREEDY, FUSION_LEARNED, FUSION_NONE, FUSION_PAULI_GROUPS, GATE_DTYPE, TERM_DTYPE,
+                   QuantIronError, check, lib)
 
 __all__ = ["DeviceState", "Plan", "circuit_execute", "sumop_expectation", "sumop_apply", "trotter_evolve",
-           "launch_count", "F32", "F64", "FUSION_NONE", "FUSION_GREEDY", "FUSION_LEARNED", "QuantIronError"]
+           "launch_count", "F32", "F64", "FUSION_NONE", "FUSION_GREEDY", "FUSION_LEARNED",
+           "FUSION_PAULI_GROUPS", "QuantIronError"]
 
 
 def launch_count():
@@ -224,6 +225,19 @@ class Plan:
                 check(lib.qi_plan_op_phase_poly(self.h, i, ctypes.byref(c0), a.ctypes.data, b.ctypes.data))
                 op["targets"] = [q for q in range(nq) if (info.zmask >> q) & 1]
                 op["poly"] = (np.uint64(c0.value), a, b.reshape(nq, nq))
+            if info.kind == 10:   # grouped Pauli exponentials: parity bases and their tables
+                nt = ctypes.c_int32()
+                rank = np.zeros(4, dtype=np.int32)
+                basis = np.zeros(32, dtype=np.uint64)
+                check(lib.qi_plan_op_pauli_group(self.h, i, ctypes.byref(nt), rank.ctypes.data, basis.ctypes.data))
+                per = 4 if info.xmask else 1
+                tables, off = [], 0
+                for t in range(nt.value):
+                    cnt = per << int(rank[t])
+                    tab = mat[off:off + cnt]
+                    tables.append((basis[8 * t:8 * t + rank[t]].copy(), tab.reshape(-1, 2, 2) if per == 4 else tab))
+                    off += cnt
+                op["group"] = tables
             out.append(op)
         return out
 
@@ -313,7 +327,8 @@ def trotter_evolve(state, terms, dt, num_steps, order=1, observable=None, observ
 
 
 KERNEL_OF_OP_KIND = {1: "k_mat1", 2: "k_swap", 3: "k_mat2", 4: "k_fused", 5: "k_pauli_exp", 6: "k_pauli_exp+normalise",
-                     7: "k_diagk", 8: "k_norm_partial+k_normalise_apply", 9: "k_phase_poly"}
+                     7: "k_diagk", 8: "k_norm_partial+k_normalise_apply", 9: "k_phase_poly",
+                     10: "k_pauli_group_diag|k_pauli_group_pair"}
 
 
 def plan_profile(plan, state):

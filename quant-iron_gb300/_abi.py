@@ -23,6 +23,7 @@ F32 = 1
 FUSION_NONE = 0
 FUSION_GREEDY = 1
 FUSION_LEARNED = 2
+FUSION_PAULI_GROUPS = 3
 MAX_CONTROLS = 32
 
 # qi_status -> name of the quant_iron::errors::Error variant (src/errors.rs:4-97)
@@ -200,5 +201,7 @@ lib.qi_sumop_expectation_noalloc.restype = _i32
 lib.qi_sumop_expectation_noalloc.argtypes = [_vp, _i32, _i32, _vp, _i64, _vp, _pd]
 lib.qi_plan_op_phase_poly.restype = _i32
 lib.qi_plan_op_phase_poly.argtypes = [_vp, _i64, ctypes.POINTER(_u64), _vp, _vp]
+lib.qi_plan_op_pauli_group.restype = _i32
+lib.qi_plan_op_pauli_group.argtypes = [_vp, _i64, ctypes.POINTER(_i32), _vp, _vp]
 lib.qi_adjoint_gradient.restype = _i32
 lib.qi_adjoint_gradient.argtypes = [_vp, _vp, _i64, _pd, _i64, _vp, _i64, ctypes.POINTER(ExecOptions), _pd, _pd]

@@ -116,11 +116,20 @@ __global__ void k_norm_partial(const typename Cx<T>::V2 *a, uint64_t dim, double
     if constexpr (sizeof(T) == 4) {
         const float4 *a4 = reinterpret_cast<const float4 *>(a);
         const uint64_t n4 = dim >> 1;
+        // FP32 sums of 8 float4 (16 amplitudes) folded into FP64: a conversion and an
+        // FP64 add per float4 would make this kernel FP64-bound on this part
+        float part = 0.0f;
+        int batch = 0;
         for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n4; i += stride) {
             float4 v = ldg_stream(a4 + i);
-            float s = fmaf(v.x, v.x, fmaf(v.y, v.y, fmaf(v.z, v.z, v.w * v.w)));
-            acc += (double)s;
+            part += fmaf(v.x, v.x, fmaf(v.y, v.y, fmaf(v.z, v.z, v.w * v.w)));
+            if (++batch == 8) {
+                acc += (double)part;
+                part = 0.0f;
+                batch = 0;
+            }
         }
+        acc += (double)part;
         if ((dim & 1) && blockIdx.x == 0 && threadIdx.x == 0) {   // dim == 1 only when n == 0
             float2 v = reinterpret_cast<const float2 *>(a)[dim - 1];
             acc += (double)v.x * v.x + (double)v.y * v.y;
@@ -183,18 +192,30 @@ __global__ void k_finalize(const double *partials, int nb, int ncomp, double *re
 // norm == 0 -> flag ZeroNorm (state untouched); norm == 1 -> untouched.
 template <typename T>
 __global__ void k_normalise_apply(typename Cx<T>::V2 *a, uint64_t dim, const double *result, int *flag) {
-    double norm = sqrt(result[0]);
-    if (norm == 0.0) {
-        if (blockIdx.x == 0 && threadIdx.x == 0) *flag = 1;
-        return;
+    // one thread per block takes the FP64 square root and reciprocal (tens of FP64
+    // operations; FP64 is the GB300's slowest pipe)
+    __shared__ T s_inv;
+    __shared__ int s_scale;
+    if (threadIdx.x == 0) {
+        const double norm = sqrt(result[0]);
+        if (norm == 0.0 && blockIdx.x == 0) *flag = 1;
+        s_scale = norm != 0.0 && norm != 1.0;
+        s_inv = (T)(1.0 / norm);
     }
-    if (norm == 1.0) return;
-    const T inv = (T)(1.0 / norm);
-    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < dim; i += (uint64_t)gridDim.x * blockDim.x) {
-        typename Cx<T>::V2 v = a[i];
-        // multiply by the reciprocal (within 1 ulp of x / norm): FP64 division is
-        // tens of FP64 operations, and FP64 is the GB300's slowest pipe
-        a[i] = Cx<T>::make(v.x * inv, v.y * inv);
+    __syncthreads();
+    if (!s_scale) return;
+    const T inv = s_inv;
+    constexpr int U = 4;
+    const uint64_t step = blockDim.x, stride = (uint64_t)gridDim.x * blockDim.x * U;
+    for (uint64_t base = blockIdx.x * (uint64_t)blockDim.x * U + threadIdx.x; base < dim; base += stride) {
+        typename Cx<T>::V2 v[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+            if (base + u * step < dim) v[u] = a[base + u * step];
+        // multiply by the reciprocal (within 1 ulp of x / norm)
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+            if (base + u * step < dim) a[base + u * step] = Cx<T>::make(v[u].x * inv, v[u].y * inv);
     }
 }
 

@@ -547,6 +547,8 @@ Status launch_op(qi_state *s, const Op &op, const void *d_mats, const void *d_tc
     }
     case OP_PAULI_EXP:
         return launch_pauli_exp(s, op.xmask, op.zmask, op.cre, op.cim, op.sre, op.sim);
+    case OP_PAULI_GROUP:
+        return launch_pauli_group(s, op, d_mats);
     case OP_PAULI_NORM: {
         Status st = launch_pauli_exp(s, op.xmask, op.zmask, 0.0, 0.0, 1.0, 0.0);   // P psi
         if (!st.ok()) return st;

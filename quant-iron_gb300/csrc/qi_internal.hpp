@@ -93,7 +93,11 @@ enum OpKind : int32_t {
     OP_DIAGK = 7,         // diagonal on k targets (2^k phases), controlled by nothing
     OP_NORMALISE = 8,     // FP64 norm on the device, divide (periodic renormalisation)
     OP_PHASE_POLY = 9,    // run of diagonal blocks as one quadratic phase polynomial over all qubits (FP32)
+    OP_PAULI_GROUP = 10,  // run of Pauli exponentials with X-masks in {0, X}: parity-indexed table, one pass
 };
+// OP_PAULI_GROUP limits: diagonal runs use up to kGroupChunks tables of up to
+// 2^kGroupRank factors; pair runs one table of up to 2^kPairRank 2x2 matrices.
+constexpr int kGroupChunks = 4, kGroupRank = 8, kPairRank = 6;
 enum Mat1Mode : int32_t { M1_GENERAL = 0, M1_DIAG = 1, M1_ANTIDIAG = 2, M1_PHASE1 = 3, M1_REAL = 4 };
 
 struct Op {
@@ -108,6 +112,11 @@ struct Op {
     uint64_t xmask = 0, zmask = 0; // Pauli ops
     double alpha_re = 0, alpha_im = 0;   // Pauli exp: cosh/sinh coefficients are derived from this
     double cre = 0, cim = 0, sre = 0, sim = 0;
+    // OP_PAULI_GROUP: table c is indexed by the parities popc(i & basis[c * kGroupRank + j]) & 1,
+    // j < rank[c] (pair groups: i = the partner with the highest bit of xmask clear)
+    int32_t nchunk = 0;
+    int32_t rank[kGroupChunks] = {0, 0, 0, 0};
+    uint64_t basis[kGroupChunks * kGroupRank] = {0};
 };
 
 // Host-side description of a gate after validation: 2x2 / 4x4 matrix on its
@@ -137,6 +146,12 @@ Status launch_op(qi_state *s, const Op &op, const void *d_mats, const void *d_tc
 Status launch_pauli_exp(qi_state *s, uint64_t xmask, uint64_t zmask, double cre, double cim, double sre, double sim);
 Status launch_pauli_apply(qi_state *out, qi_state *in, uint64_t xmask, uint64_t zmask, double cre, double cim);
 Status validate_pauli(int n, const qi_pauli_term &t);
+// Group the Pauli exponentials run[start..] (exp(alpha P) each) into one
+// OP_PAULI_GROUP op, its tables appended to `mats`.  Returns how many terms
+// the op covers; 1 means no group formed (op untouched; lower the term alone).
+size_t pauli_group_op(const std::vector<const GateMatrix *> &run, size_t start, Op &op,
+                      std::vector<std::complex<double>> &mats);
+Status launch_pauli_group(qi_state *s, const Op &op, const void *d_mats);
 
 // ------------------------------------------------------------------ fused --
 // Apply a dense 2^k x 2^k complex matrix (device pointer, row-major, element

@@ -40,16 +40,31 @@ struct ExpParams {
     double sre, sim;   // sinh(alpha) * (-i)^ny
 };
 
-// Diagonal case (xmask == 0): psi_i *= cosh + sinh * (-1)^popc(i & z).
+// Amplitudes (or pairs) a thread keeps in flight per loop step: one load per
+// step leaves too few bytes in flight to cover HBM latency at full occupancy.
+template <typename T> struct Unroll { static constexpr int kDiag = 8, kPair = 2; };
+template <> struct Unroll<double> { static constexpr int kDiag = 4, kPair = 2; };
+
+// Diagonal case (xmask == 0): psi_i *= cosh + sinh * (-1)^popc(i & z).  The two
+// factors arrive in the state's precision: computed in the kernel from the FP64
+// coefficients, the compiler may move the FP64 add and conversion into the
+// per-amplitude select, which makes the FP32 kernel FP64-bound on this part.
 template <typename T>
-__global__ void __launch_bounds__(256) k_pauli_exp_diag(typename Cx<T>::V2 *a, ExpParams p) {
+__global__ void __launch_bounds__(256) k_pauli_exp_diag(typename Cx<T>::V2 *a, uint64_t nwork, uint64_t zmask,
+                                                        typename Cx<T>::V2 plus, typename Cx<T>::V2 minus) {
     using X = Cx<T>;
-    const typename X::V2 plus = X::make((T)(p.cre + p.sre), (T)(p.cim + p.sim));
-    const typename X::V2 minus = X::make((T)(p.cre - p.sre), (T)(p.cim - p.sim));
-    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < p.nwork; i += stride) {
-        typename X::V2 v = a[i];
-        a[i] = X::mul((__popcll(i & p.zmask) & 1) ? minus : plus, v);
+    constexpr int U = Unroll<T>::kDiag;
+    const uint64_t step = (uint64_t)blockDim.x, stride = (uint64_t)gridDim.x * blockDim.x * U;
+    for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x * U + threadIdx.x; base < nwork; base += stride) {
+        typename X::V2 v[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+            if (base + u * step < nwork) v[u] = a[base + u * step];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const uint64_t i = base + u * step;
+            if (i < nwork) a[i] = X::mul((__popcll(i & zmask) & 1) ? minus : plus, v[u]);
+        }
     }
 }
 
@@ -58,20 +73,34 @@ __global__ void __launch_bounds__(256) k_pauli_exp_diag(typename Cx<T>::V2 *a, E
 // costs 4 FP64 operations instead of 8 (FP64 arithmetic bounds this kernel here).
 template <bool SIMAG>
 __global__ void __launch_bounds__(256) k_pauli_exp_pair_real64(double2 *a, ExpParams p) {
+    constexpr int U = Unroll<double>::kPair;
     const double c = p.cre, s = SIMAG ? p.sim : p.sre;
-    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    const uint64_t step = (uint64_t)blockDim.x, stride = (uint64_t)gridDim.x * blockDim.x * U;
     const uint64_t lo_mask = p.hbit - 1;
-    for (uint64_t w = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; w < p.nwork; w += stride) {
-        const uint64_t i = ((w & ~lo_mask) << 1) | (w & lo_mask);
-        const uint64_t j = i ^ p.xmask;
-        const double2 x = a[i], y = a[j];
-        const double si = (__popcll(i & p.zmask) & 1) ? -s : s, sj = (__popcll(j & p.zmask) & 1) ? -s : s;
-        if (SIMAG) {   // c x + i s y
-            a[i] = make_double2(::fma(-si, y.y, c * x.x), ::fma(si, y.x, c * x.y));
-            a[j] = make_double2(::fma(-sj, x.y, c * y.x), ::fma(sj, x.x, c * y.y));
-        } else {       // c x + s y
-            a[i] = make_double2(::fma(si, y.x, c * x.x), ::fma(si, y.y, c * x.y));
-            a[j] = make_double2(::fma(sj, x.x, c * y.x), ::fma(sj, x.y, c * y.y));
+    for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x * U + threadIdx.x; base < p.nwork; base += stride) {
+        double2 x[U], y[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const uint64_t w = base + u * step;
+            if (w < p.nwork) {
+                const uint64_t i = ((w & ~lo_mask) << 1) | (w & lo_mask);
+                x[u] = a[i];
+                y[u] = a[i ^ p.xmask];
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const uint64_t w = base + u * step;
+            if (w >= p.nwork) continue;
+            const uint64_t i = ((w & ~lo_mask) << 1) | (w & lo_mask), j = i ^ p.xmask;
+            const double si = (__popcll(i & p.zmask) & 1) ? -s : s, sj = (__popcll(j & p.zmask) & 1) ? -s : s;
+            if (SIMAG) {   // c x + i s y
+                a[i] = make_double2(::fma(-si, y[u].y, c * x[u].x), ::fma(si, y[u].x, c * x[u].y));
+                a[j] = make_double2(::fma(-sj, x[u].y, c * y[u].x), ::fma(sj, x[u].x, c * y[u].y));
+            } else {       // c x + s y
+                a[i] = make_double2(::fma(si, y[u].x, c * x[u].x), ::fma(si, y[u].y, c * x[u].y));
+                a[j] = make_double2(::fma(sj, x[u].x, c * y[u].x), ::fma(sj, x[u].y, c * y[u].y));
+            }
         }
     }
 }
@@ -124,6 +153,113 @@ __global__ void __launch_bounds__(256) k_pauli_gather(typename Cx<T>::V2 *o, con
         o[i] = X::mul((__popcll(i & zmask) & 1) ? fn : f, in[i ^ xmask]);
 }
 
+// ------------------------------------------------------------------------
+// Grouped exponentials (OP_PAULI_GROUP).  A run of exponentials whose X-masks
+// all lie in {0, X} maps each pair (i0, i1 = i0 ^ X) (each amplitude, X = 0)
+// to itself, and every factor depends on i0 only through the parities
+// popc(i0 & z_k) & 1.  Those parities are XORs of r basis parities
+// beta_j = popc(i0 & w_j) & 1, so the whole run is one 2x2 matrix (one
+// factor) per beta in [0, 2^r): a table built on the host, applied in one
+// pass.  Diagonal runs split into up to kGroupChunks tables (factors commute).
+struct GroupParams {
+    uint64_t nwork;            // amplitudes (diagonal) or pairs
+    uint64_t xmask, lo_mask;   // pair groups: partner mask; bits below its highest bit
+    int32_t nchunk, ntab;      // tables and their total entries (complex)
+    int32_t nbytes;            // index bytes (ceil(n / 8))
+    int32_t rank[kGroupChunks];
+    int32_t off[kGroupChunks];
+    uint64_t basis[kGroupChunks * kGroupRank];
+};
+
+// Parities are a GF(2)-linear map of the index, so they are gathered per index
+// byte: ptab[b][v] packs, at bit 8c + j, the parity of (v << 8b) & basis[c][j];
+// the parities of i are the XOR of ptab[b][byte b of i] over its bytes.
+constexpr int kParityBytes = 5;   // indices up to 40 bits
+
+__device__ __forceinline__ void build_parity_bytes(uint32_t *ptab, const GroupParams &p) {
+    for (int e = threadIdx.x; e < p.nbytes * 256; e += blockDim.x) {
+        const uint64_t v = (uint64_t)(e & 255) << (8 * (e >> 8));
+        uint32_t word = 0;
+        for (int c = 0; c < p.nchunk; ++c)
+            for (int j = 0; j < p.rank[c]; ++j)
+                word |= (uint32_t)(__popcll(v & p.basis[c * kGroupRank + j]) & 1) << (8 * c + j);
+        ptab[e] = word;
+    }
+}
+
+template <typename IDX>
+__device__ __forceinline__ uint32_t parity_word(IDX i, const uint32_t *ptab, int nbytes) {
+    uint32_t word = ptab[(uint32_t)i & 255u];
+#pragma unroll
+    for (int b = 1; b < kParityBytes; ++b)
+        if (b < nbytes) word ^= ptab[b * 256 + (uint32_t)(((uint64_t)i >> (8 * b)) & 255u)];
+    return word;
+}
+
+template <typename T, typename IDX>
+__global__ void __launch_bounds__(256) k_pauli_group_diag(typename Cx<T>::V2 *a, const __grid_constant__ GroupParams p,
+                                                          const typename Cx<T>::V2 *tab) {
+    using X = Cx<T>;
+    constexpr int U = Unroll<T>::kDiag;
+    __shared__ typename X::V2 st[kGroupChunks << kGroupRank];
+    __shared__ uint32_t ptab[kParityBytes * 256];
+    for (int k = threadIdx.x; k < p.ntab; k += blockDim.x) st[k] = tab[k];
+    build_parity_bytes(ptab, p);
+    __syncthreads();
+    const IDX nwork = (IDX)p.nwork, step = (IDX)blockDim.x, stride = (IDX)gridDim.x * blockDim.x * U;
+    for (IDX base = (IDX)blockIdx.x * blockDim.x * U + threadIdx.x; base < nwork; base += stride) {
+        typename X::V2 v[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+            if (base + u * step < nwork) v[u] = a[base + u * step];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const IDX i = base + u * step;
+            if (i >= nwork) continue;
+            const uint32_t word = parity_word(i, ptab, p.nbytes);
+            typename X::V2 f = st[word & 255u];
+            for (int c = 1; c < p.nchunk; ++c) f = X::mul(f, st[p.off[c] + ((word >> (8 * c)) & 255u)]);
+            a[i] = X::mul(f, v[u]);
+        }
+    }
+}
+
+// Pair groups: table entry beta holds (m00, m01, m10, m11); new (psi_i0, psi_i1) = M (psi_i0, psi_i1).
+template <typename T, typename IDX>
+__global__ void __launch_bounds__(256) k_pauli_group_pair(typename Cx<T>::V2 *a, const __grid_constant__ GroupParams p,
+                                                          const typename Cx<T>::V2 *tab) {
+    using X = Cx<T>;
+    constexpr int U = Unroll<T>::kPair;
+    __shared__ typename X::V2 st[4 << kPairRank];
+    __shared__ uint32_t ptab[kParityBytes * 256];
+    for (int k = threadIdx.x; k < p.ntab; k += blockDim.x) st[k] = tab[k];
+    build_parity_bytes(ptab, p);
+    __syncthreads();
+    const IDX nwork = (IDX)p.nwork, step = (IDX)blockDim.x, stride = (IDX)gridDim.x * blockDim.x * U;
+    const IDX lo = (IDX)p.lo_mask, xm = (IDX)p.xmask;
+    for (IDX base = (IDX)blockIdx.x * blockDim.x * U + threadIdx.x; base < nwork; base += stride) {
+        typename X::V2 x[U], y[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const IDX w = base + u * step;
+            if (w < nwork) {
+                const IDX i = ((w & ~lo) << 1) | (w & lo);
+                x[u] = a[i];
+                y[u] = a[i ^ xm];
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const IDX w = base + u * step;
+            if (w >= nwork) continue;
+            const IDX i = ((w & ~lo) << 1) | (w & lo);
+            const typename X::V2 *m = st + 4 * parity_word(i, ptab, p.nbytes);
+            a[i] = X::fma(m[1], y[u], X::mul(m[0], x[u]));
+            a[i ^ xm] = X::fma(m[3], y[u], X::mul(m[2], x[u]));
+        }
+    }
+}
+
 static unsigned pgrid(uint64_t work) {
     uint64_t g = (work + 255) / 256;
     if (g < 1) g = 1;
@@ -145,8 +281,14 @@ Status launch_pauli_exp(qi_state *s, uint64_t xmask, uint64_t zmask, double cre,
     if (xmask == 0) {
         p.nwork = s->dim();
         unsigned g = pgrid(p.nwork);
-        if (f32) k_pauli_exp_diag<float><<<g, 256, 0, s->stream>>>((float2 *)s->amps, p);
-        else k_pauli_exp_diag<double><<<g, 256, 0, s->stream>>>((double2 *)s->amps, p);
+        const double pr = p.cre + p.sre, pi = p.cim + p.sim, mr = p.cre - p.sre, mi = p.cim - p.sim;
+        if (f32)
+            k_pauli_exp_diag<float><<<g, 256, 0, s->stream>>>((float2 *)s->amps, p.nwork, zmask,
+                                                              make_float2((float)pr, (float)pi),
+                                                              make_float2((float)mr, (float)mi));
+        else
+            k_pauli_exp_diag<double><<<g, 256, 0, s->stream>>>((double2 *)s->amps, p.nwork, zmask,
+                                                               make_double2(pr, pi), make_double2(mr, mi));
         count_launch();
         return check_launch("k_pauli_exp_diag");
     }
@@ -169,6 +311,175 @@ Status launch_pauli_exp(qi_state *s, uint64_t xmask, uint64_t zmask, double cre,
     }
     count_launch();
     return check_launch("k_pauli_exp_pair");
+}
+
+// GF(2) basis of parity masks: each placed mask is the XOR of a subset of the
+// basis masks w[j] (kept with a row-echelon copy for the reduction).
+struct ParityBasis {
+    int r = 0;
+    uint64_t w[kGroupRank] = {0}, ech[kGroupRank] = {0};
+    uint32_t comb[kGroupRank] = {0};
+    int piv[kGroupRank] = {0};
+    // subset of w whose XOR is z; adds z as a basis mask when independent and r < cap
+    bool place(uint64_t z, int cap, uint32_t *subset) {
+        uint32_t c = 0;
+        uint64_t v = z;
+        for (int j = 0; j < r; ++j)
+            if ((v >> piv[j]) & 1ull) { v ^= ech[j]; c ^= comb[j]; }
+        if (v == 0) { *subset = c; return true; }
+        if (r >= cap) return false;
+        piv[r] = 63 - __builtin_clzll(v);
+        ech[r] = v;
+        comb[r] = c ^ (1u << r);
+        w[r] = z;
+        *subset = 1u << r;
+        ++r;
+        return true;
+    }
+};
+
+using cd = std::complex<double>;
+
+// cosh(alpha) and sinh(alpha) * (-i)^ny of exp(alpha P) (the factors launch_pauli_exp uses)
+static void exp_factors(const GateMatrix &g, cd *ch, cd *sh) {
+    const double ar = g.alpha_re, ai = g.alpha_im;
+    *ch = cd(std::cosh(ar) * std::cos(ai), std::sinh(ar) * std::sin(ai));
+    double pr, pi;
+    minus_i_pow(__builtin_popcountll(g.xmask & g.zmask), pr, pi);
+    *sh = cd(std::sinh(ar) * std::cos(ai), std::cosh(ar) * std::sin(ai)) * cd(pr, pi);
+}
+
+size_t pauli_group_op(const std::vector<const GateMatrix *> &run, size_t start, Op &op, std::vector<cd> &mats) {
+    const GateMatrix &g0 = *run[start];
+    std::vector<std::pair<size_t, uint32_t>> members;   // (term, subset of basis parities), application order
+    if (g0.xmask == 0) {
+        // diagonal run: factors commute, so each term joins any table that can index it
+        ParityBasis chunk[kGroupChunks];
+        std::vector<int> which;
+        int nchunk = 0;
+        size_t k = start;
+        for (; k < run.size() && run[k]->xmask == 0; ++k) {
+            uint32_t sub = 0;
+            int c = 0;
+            for (; c < nchunk; ++c)   // a table that indexes the term without a new basis mask
+                if (chunk[c].place(run[k]->zmask, chunk[c].r, &sub)) break;
+            if (c == nchunk) {        // else the first table with room for one
+                for (c = 0; c < nchunk; ++c)
+                    if (chunk[c].place(run[k]->zmask, kGroupRank, &sub)) break;
+                if (c == nchunk) {
+                    if (nchunk == kGroupChunks) break;   // the run continues in the next group
+                    chunk[nchunk++].place(run[k]->zmask, kGroupRank, &sub);
+                }
+            }
+            members.emplace_back(k, sub);
+            which.push_back(c);
+        }
+        const size_t count = k - start;
+        if (count < 2) return 1;
+        op = Op();
+        op.kind = OP_PAULI_GROUP;
+        op.k = (int32_t)count;
+        op.nchunk = nchunk;
+        op.mat_offset = (int64_t)mats.size();
+        for (int c = 0; c < nchunk; ++c) {
+            op.rank[c] = chunk[c].r;
+            for (int j = 0; j < chunk[c].r; ++j) {
+                op.basis[c * kGroupRank + j] = chunk[c].w[j];
+                op.zmask |= chunk[c].w[j];
+            }
+            std::vector<cd> tab((size_t)1 << chunk[c].r, cd(1.0, 0.0));
+            for (size_t m = 0; m < members.size(); ++m) {
+                if (which[m] != c) continue;
+                cd ch, sh;
+                exp_factors(*run[members[m].first], &ch, &sh);
+                for (size_t b = 0; b < tab.size(); ++b)
+                    tab[b] *= (__builtin_popcount((uint32_t)b & members[m].second) & 1) ? ch - sh : ch + sh;
+            }
+            mats.insert(mats.end(), tab.begin(), tab.end());
+        }
+        return count;
+    }
+    // pair run: every X-mask is 0 or X; parities are taken on i0 (highest bit of X clear)
+    const uint64_t X = g0.xmask, hb = 1ull << (63 - __builtin_clzll(X));
+    ParityBasis basis;
+    size_t k = start;
+    for (; k < run.size() && (run[k]->xmask == 0 || run[k]->xmask == X); ++k) {
+        uint32_t sub = 0;
+        if (!basis.place(run[k]->zmask & ~hb, kPairRank, &sub)) break;
+        members.emplace_back(k, sub);
+    }
+    const size_t count = k - start;
+    if (count < 2) return 1;
+    op = Op();
+    op.kind = OP_PAULI_GROUP;
+    op.k = (int32_t)count;
+    op.nchunk = 1;
+    op.rank[0] = basis.r;
+    op.xmask = X;
+    for (int j = 0; j < basis.r; ++j) {
+        op.basis[j] = basis.w[j];
+        op.zmask |= basis.w[j];
+    }
+    op.mat_offset = (int64_t)mats.size();
+    for (uint32_t b = 0; b < (1u << basis.r); ++b) {
+        cd m[4] = {1.0, 0.0, 0.0, 1.0};
+        for (const auto &mem : members) {
+            const GateMatrix &g = *run[mem.first];
+            cd ch, sh;
+            exp_factors(g, &ch, &sh);
+            const int p0 = __builtin_popcount(b & mem.second) & 1;
+            const int p1 = p0 ^ (__builtin_popcountll(X & g.zmask) & 1);
+            const cd s0 = p0 ? -sh : sh, s1 = p1 ? -sh : sh;
+            cd t[4];
+            if (g.xmask == 0) { t[0] = ch + s0; t[1] = 0.0; t[2] = 0.0; t[3] = ch + s1; }
+            else { t[0] = ch; t[1] = s0; t[2] = s1; t[3] = ch; }
+            const cd r0 = t[0] * m[0] + t[1] * m[2], r1 = t[0] * m[1] + t[1] * m[3];
+            const cd r2 = t[2] * m[0] + t[3] * m[2], r3 = t[2] * m[1] + t[3] * m[3];
+            m[0] = r0; m[1] = r1; m[2] = r2; m[3] = r3;
+        }
+        mats.insert(mats.end(), m, m + 4);
+    }
+    return count;
+}
+
+Status launch_pauli_group(qi_state *s, const Op &op, const void *d_mats) {
+    GroupParams p;
+    std::memset(&p, 0, sizeof(p));
+    p.xmask = op.xmask;
+    p.nchunk = op.nchunk;
+    int32_t ntab = 0;
+    for (int c = 0; c < op.nchunk; ++c) {
+        p.rank[c] = op.rank[c];
+        p.off[c] = ntab;
+        ntab += (op.xmask ? 4 : 1) << op.rank[c];
+        for (int j = 0; j < op.rank[c]; ++j) p.basis[c * kGroupRank + j] = op.basis[c * kGroupRank + j];
+    }
+    p.ntab = ntab;
+    p.nbytes = (s->n + 7) / 8;
+    const bool f32 = s->prec == QI_F32;
+    const size_t esz = f32 ? sizeof(float2) : sizeof(double2);
+    const void *tab = (const char *)d_mats + (size_t)op.mat_offset * esz;
+    const bool narrow = s->dim() <= (1ull << 31);   // 32-bit indices
+    if (op.xmask == 0) {
+        p.nwork = s->dim();
+        const unsigned g = pgrid(p.nwork);
+#define QI_GD(T, I) k_pauli_group_diag<T, I><<<g, 256, 0, s->stream>>>((Cx<T>::V2 *)s->amps, p, (const Cx<T>::V2 *)tab)
+        if (f32) { if (narrow) QI_GD(float, uint32_t); else QI_GD(float, uint64_t); }
+        else { if (narrow) QI_GD(double, uint32_t); else QI_GD(double, uint64_t); }
+#undef QI_GD
+        count_launch();
+        return check_launch("k_pauli_group_diag");
+    }
+    const uint64_t hb = 1ull << (63 - __builtin_clzll(op.xmask));
+    p.lo_mask = hb - 1;
+    p.nwork = s->dim() >> 1;
+    const unsigned g = pgrid(p.nwork);
+#define QI_GP(T, I) k_pauli_group_pair<T, I><<<g, 256, 0, s->stream>>>((Cx<T>::V2 *)s->amps, p, (const Cx<T>::V2 *)tab)
+    if (f32) { if (narrow) QI_GP(float, uint32_t); else QI_GP(float, uint64_t); }
+    else { if (narrow) QI_GP(double, uint32_t); else QI_GP(double, uint64_t); }
+#undef QI_GP
+    count_launch();
+    return check_launch("k_pauli_group_pair");
 }
 
 Status launch_pauli_apply(qi_state *out, qi_state *in, uint64_t xmask, uint64_t zmask, double cre, double cim) {

@@ -8,7 +8,9 @@
 //   QI_FUSION_NONE   one streaming kernel per gate (the plain per-gate method);
 //   QI_FUSION_GREEDY the greedy fuser below with block width k;
 //   QI_FUSION_LEARNED candidate partitions scored by the learned cost model
-//                    (qi_costmodel.cu), greedy as the fallback.
+//                    (qi_costmodel.cu), greedy as the fallback;
+//   QI_FUSION_PAULI_GROUPS per gate, but runs of Pauli exponentials with X-masks
+//                    in {0, X} become one grouped pass each (qi_pauli.cu).
 //
 // Greedy fuser ("light-cone" absorption).  A block starts empty; the
 // remaining gates are scanned in order.  A gate joins the block when its
@@ -240,8 +242,31 @@ Status build_plan(qi_plan *p, std::vector<Elem> &elems) {
             p->stats.n_blocks_by_k[0]++;
         }
     };
-    if (fusion == QI_FUSION_NONE) {
-        for (const Elem &e : elems) lower_single(e);
+    if (fusion == QI_FUSION_NONE || fusion == QI_FUSION_PAULI_GROUPS) {
+        auto groupable = [&](const Elem &e) {
+            return fusion == QI_FUSION_PAULI_GROUPS && e.pauli && !e.gm.normalise_after;
+        };
+        for (size_t i = 0; i < elems.size();) {
+            if (!groupable(elems[i])) {
+                lower_single(elems[i++]);
+                continue;
+            }
+            std::vector<const GateMatrix *> run;
+            size_t j = i;
+            for (; j < elems.size() && groupable(elems[j]); ++j) run.push_back(&elems[j].gm);
+            for (size_t used = 0; used < run.size();) {
+                Op op;
+                const size_t took = pauli_group_op(run, used, op, p->mats);
+                if (took == 1) {
+                    lower_single(elems[i + used]);
+                } else {
+                    p->ops.push_back(op);
+                    p->stats.n_blocks_by_k[0]++;
+                }
+                used += took;
+            }
+            i = j;
+        }
     } else {
         std::vector<Block> blocks = p->partition_override.empty() ? choose_partition(p, elems, kmax)
                                                                   : p->partition_override;
@@ -577,6 +602,17 @@ qi_status qi_plan_op_phase_poly(const qi_plan *p, int64_t i, uint64_t *c0, uint6
     return publish(ok_status());
 }
 
+qi_status qi_plan_op_pauli_group(const qi_plan *p, int64_t i, int32_t *n_tables, int32_t *rank, uint64_t *basis) {
+    if (!p || !n_tables || !rank || !basis) return publish(err(QI_ERR_NULL_ARGUMENT));
+    if (i < 0 || i >= (int64_t)p->ops.size()) return publish(err(QI_ERR_INVALID_INPUT_VALUE, i));
+    const Op &op = p->ops[(size_t)i];
+    if (op.kind != OP_PAULI_GROUP) return publish(err(QI_ERR_INVALID_INPUT_VALUE, i, op.kind, "not a Pauli-group op"));
+    *n_tables = op.nchunk;
+    std::copy(op.rank, op.rank + kGroupChunks, rank);
+    std::copy(op.basis, op.basis + kGroupChunks * kGroupRank, basis);
+    return publish(ok_status());
+}
+
 qi_status qi_plan_op_get(const qi_plan *p, int64_t i, qi_plan_op_info *info, double *matrix_out, int64_t capacity) {
     if (!p || !info) return publish(err(QI_ERR_NULL_ARGUMENT));
     if (i < 0 || i >= (int64_t)p->ops.size()) return publish(err(QI_ERR_INVALID_INPUT_VALUE, i));
@@ -603,6 +639,15 @@ qi_status qi_plan_op_get(const qi_plan *p, int64_t i, qi_plan_op_info *info, dou
         break;
     }
     case OP_PAULI_EXP: m = {op.cre, op.cim, op.sre, op.sim}; break;
+    case OP_PAULI_GROUP: {
+        size_t cnt = 0;
+        for (int c = 0; c < op.nchunk; ++c) cnt += (size_t)(op.xmask ? 4 : 1) << op.rank[c];
+        for (size_t j = 0; j < cnt; ++j) {
+            m.push_back(p->mats[(size_t)op.mat_offset + j].real());
+            m.push_back(p->mats[(size_t)op.mat_offset + j].imag());
+        }
+        break;
+    }
     default: break;
     }
     info->n_matrix = (int64_t)(m.size() / 2);
@@ -671,14 +716,16 @@ qi_status qi_trotter_evolve(qi_state *s, const qi_pauli_term *terms, int64_t n_t
     // polynomials.  With real coefficients every exponential is unitary, so the
     // plan may use the tensor-core blocks and renormalise once per step; complex
     // coefficients (a non-unitary step) keep the CUDA-core blocks and the norm.
-    // FP64: one memory-bound pass per exponential (FP64 arithmetic is scarce on
-    // this part, so dense FP64 blocks would be compute-bound).
+    // FP64: FP64 arithmetic is scarce on this part (dense FP64 blocks would be
+    // compute-bound), so each run of exponentials whose X-masks lie in {0, X}
+    // (e.g. the XX, YY, ZZ terms of one bond, or a run of Z fields) is one pass
+    // with a parity-indexed table; other terms are one pass each.
     bool unitary = true;
     for (int64_t k = 0; k < n_terms; ++k) unitary = unitary && terms[k].coeff_im == 0.0;
     qi_plan plan;
     plan.n = s->n;
     plan.prec = s->prec;
-    plan.opts.fusion = s->prec == QI_F32 ? QI_FUSION_GREEDY : QI_FUSION_NONE;
+    plan.opts.fusion = s->prec == QI_F32 ? QI_FUSION_GREEDY : QI_FUSION_PAULI_GROUPS;
     plan.opts.use_tensor_cores = unitary ? 1 : 2;
     plan.opts.renorm_every = unitary ? 0 : -1;
     plan.opts.max_block_qubits = 0;

@@ -132,3 +132,74 @@ def test_pauli_normalised_gate(qi, orc):
         st.upload(init)
         qi.pauli_apply_normalised(st, t)
         assert np.max(np.abs(st.download() - orc.pauli_apply_normalised(init, n, t))) < 1e-12
+
+
+def _evolution_gates(terms, t):
+    gl = workloads.GateList()
+    for r in terms:
+        gl.add("PAULI_EVOLUTION", [], [], [r["re"], r["im"], t], xmask=int(r["xmask"]), zmask=int(r["zmask"]))
+    return gl.array()
+
+
+def _random_runs(n, count, seed):
+    """Exponentials with X-masks drawn from {0, X1, X2} and a long diagonal stretch."""
+    rng = np.random.default_rng(seed)
+    xs = [0, int(rng.integers(1, 1 << n)), int(rng.integers(1, 1 << n))]
+    t = np.zeros(count, dtype=workloads.TERM_DTYPE)
+    for k in range(count):
+        t[k]["re"] = rng.normal()
+        t[k]["xmask"] = 0 if count // 4 <= k < count // 2 else xs[int(rng.integers(0, 3))]
+        t[k]["zmask"] = int(rng.integers(0, 1 << n))
+    return t
+
+
+@pytest.mark.parametrize("prec", [0, 1], ids=["f64", "f32"])
+@pytest.mark.parametrize("n", [3, 11, 18])
+def test_grouped_exponentials_on_device(qi, orc, prec, n):
+    """QI_FUSION_PAULI_GROUPS plans (table-driven diagonal and pair passes) vs the
+    oracle's term-by-term exponentials; also the 5x6-shaped lattices' run structure."""
+    terms = _random_runs(n, 90, seed=n)
+    gates = _evolution_gates(terms, 0.11)
+    init = rand_state(n, 3)
+    want = orc.execute(init, n, gates)
+    plan = qi.Plan(n, prec, gates, fusion=qi.FUSION_PAULI_GROUPS)
+    assert any(op["kind"] == 10 for op in plan.ops())
+    with qi.DeviceState(n, prec) as st:
+        st.upload(init)
+        plan.execute(st)
+        got = st.download()
+    assert np.max(np.abs(got - want)) < (1e-12 if prec == 0 else 2e-5)
+
+
+@pytest.mark.parametrize("order", [1, 2])
+@pytest.mark.parametrize("lattice", ["tfim", "xxz"])
+def test_trotter_fp64_grouped_vs_oracle(qi, orc, lattice, order):
+    """FP64 Trotter steps run as grouped exponentials (one pass per bond / field run)."""
+    if lattice == "tfim":
+        n, terms = 12, workloads.lattice_tfim(3, 4, seed=1)
+    else:
+        n, terms = 12, workloads.xxz_periodic(12, seed=2)
+    init = workloads.basis_state(n, 0b101101001101)
+    want = orc.trotter(init, n, terms, 0.04, 5, order)
+    with qi.DeviceState(n, 0) as st:
+        st.upload(init)
+        qi.trotter_evolve(st, terms, 0.04, 5, order=order)
+        got = st.download()
+    assert np.max(np.abs(got - want)) < 1e-11
+
+
+def test_grouped_exponentials_32_qubits_round_trip(qi):
+    """2^32 amplitudes (64-bit index arithmetic in the grouped kernels): the run
+    followed by its inverse (reversed order, -t) returns |+...+> (FP32, 32 GiB each)."""
+    n = 32
+    terms = _random_runs(n, 24, seed=9)
+    fwd = qi.Plan(n, qi.F32, _evolution_gates(terms, 0.13), fusion=qi.FUSION_PAULI_GROUPS)
+    back = qi.Plan(n, qi.F32, _evolution_gates(terms[::-1].copy(), -0.13), fusion=qi.FUSION_PAULI_GROUPS)
+    assert sum(op["kind"] == 10 for op in fwd.ops()) >= 2
+    with qi.DeviceState(n, qi.F32) as st, qi.DeviceState(n, qi.F32) as ref:
+        st.set_plus()
+        ref.set_plus()
+        fwd.execute(st)
+        assert abs(st.inner_product(ref)) < 0.999   # the run moved the state
+        back.execute(st)
+        assert abs(st.inner_product(ref) - 1.0) < 1e-4

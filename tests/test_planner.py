@@ -74,9 +74,39 @@ def replay(ops, n, init):
             ny = bin(x & z).count("1")
             ph = (-1j) ** ny * np.where(np.array([bin(i & z).count("1") % 2 for i in idx]) == 1, -1, 1)
             s = ch * s + sh * ph * s[idx ^ x]
+        elif kind == 10:
+            s = _replay_pauli_group(s, n, op)
         else:
             raise AssertionError("unexpected op kind %d" % kind)
     return s
+
+
+def _parities(basis, idx):
+    """Table index of every entry of `idx`: bit j = popcount(idx & basis[j]) & 1."""
+    out = np.zeros(idx.size, dtype=np.int64)
+    for j, w in enumerate(basis):
+        out |= (np.bitwise_count(idx & np.uint64(w)).astype(np.int64) & 1) << j
+    return out
+
+
+def _replay_pauli_group(s, n, op):
+    idx = np.arange(1 << n, dtype=np.uint64)
+    x = int(op["xmask"])
+    if x == 0:
+        f = np.ones(1 << n, dtype=complex)
+        for basis, tab in op["group"]:
+            f *= tab[_parities(basis, idx)]
+        return s * f
+    hb = np.uint64(1 << (x.bit_length() - 1))
+    i0 = idx[(idx & hb) == 0]
+    i1 = i0 ^ np.uint64(x)
+    (basis, tab), = op["group"]
+    m = tab[_parities(basis, i0)]
+    a0, a1 = s[i0], s[i1]
+    out = s.copy()
+    out[i0] = m[:, 0, 0] * a0 + m[:, 0, 1] * a1
+    out[i1] = m[:, 1, 0] * a0 + m[:, 1, 1] * a1
+    return out
 
 
 @pytest.mark.parametrize("kmax", [2, 3, 4, 5, 6])
@@ -215,3 +245,68 @@ def test_phase_polynomial_rejects_degree_three(qi, orc):
     assert ops[1]["targets"] == [2, 3, 4]
     got = replay(ops, n, init)
     assert np.max(np.abs(got - orc.execute(init, n, gates))) < 1e-12
+
+
+def _evolution_gates(terms, t):
+    gl = workloads.GateList()
+    for r in terms:
+        gl.add("PAULI_EVOLUTION", [], [], [r["re"], r["im"], t], xmask=int(r["xmask"]), zmask=int(r["zmask"]))
+    return gl.array()
+
+
+@pytest.mark.parametrize("lattice", ["xyz", "tfim", "xxz"])
+def test_grouped_exponentials_replay_matches_oracle(qi, orc, lattice):
+    """QI_FUSION_PAULI_GROUPS: each run of exponentials with X-masks in {0, X} is one
+    table-driven op; replayed in numpy it equals the oracle's term-by-term result."""
+    if lattice == "xyz":
+        n, terms = 9, workloads.lattice_xyz(3, 3, seed=3)
+    elif lattice == "tfim":
+        n, terms = 9, workloads.lattice_tfim(3, 3, seed=3)
+    else:
+        n, terms = 8, workloads.xxz_periodic(8, seed=3)
+    gates = _evolution_gates(terms, 0.07)
+    init = workloads.basis_state(n, 0b10110101 & ((1 << n) - 1)).astype(complex)
+    init = orc.execute(init, n, workloads.random_circuit(n, layers=2, seed=4))
+    want = orc.execute(init, n, gates)
+    plan = qi.Plan(n, qi.F64, gates, fusion=qi.FUSION_PAULI_GROUPS)
+    ops = plan.ops()
+    assert len(ops) < len(gates)
+    assert {op["kind"] for op in ops} <= {5, 10}
+    got = replay(ops, n, init)
+    assert np.max(np.abs(got - want)) < 1e-12
+    assert sum(op["k"] if op["kind"] == 10 else 1 for op in ops) == len(gates)
+    if lattice == "xyz":
+        # 12 bonds (XX, YY, ZZ: one pair op each, one parity bit); the last bond's op
+        # also takes Z fields until its table would need more than 2^6 entries; the rest:
+        # one diagonal op
+        kinds = [op["kind"] for op in ops]
+        assert kinds == [10] * 13 and ops[-1]["xmask"] == 0
+        assert all(op["k"] == 3 and len(op["group"][0][0]) == 1 for op in ops[:11])
+        assert ops[11]["k"] > 3 and ops[11]["k"] + ops[12]["k"] == 3 + 9
+        assert len(ops[11]["group"][0][0]) == 6
+
+
+@pytest.mark.parametrize("seed", [0, 1, 2])
+def test_grouped_exponentials_random_runs(qi, orc, seed):
+    """Random runs: X-masks drawn from {0, X1, X2}, random Z-masks and coefficients,
+    long diagonal runs that overflow one table and the four-table limit, a term whose
+    Z-mask is 0.  (Gate::PauliTimeEvolution takes real coefficients; complex ones, whose
+    factors are not unitary, are covered through the Trotter entry point on the GPU.)"""
+    n = 10
+    rng = np.random.default_rng(seed)
+    xs = [0, int(rng.integers(1, 1 << n)), int(rng.integers(1, 1 << n))]
+    rows = []
+    for k in range(140):
+        x = 0 if 40 <= k < 110 else xs[int(rng.integers(0, 3))]
+        z = int(rng.integers(0, 1 << n)) if k != 5 else 0
+        r = np.zeros((), dtype=qi.TERM_DTYPE)
+        r["re"], r["xmask"], r["zmask"] = rng.normal(), x, z
+        rows.append(r)
+    terms = np.array(rows, dtype=qi.TERM_DTYPE)
+    gates = _evolution_gates(terms, 0.09)
+    init = workloads.plus_state(n).astype(complex)
+    want = orc.execute(init, n, gates)
+    ops = qi.Plan(n, qi.F64, gates, fusion=qi.FUSION_PAULI_GROUPS).ops()
+    assert any(op["kind"] == 10 and op["xmask"] == 0 and len(op["group"]) == 4 for op in ops)
+    got = replay(ops, n, init)
+    assert np.max(np.abs(got - want)) < 1e-12

@@ -43,7 +43,7 @@ def parse():
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
     ap.add_argument("--qubits", type=int, default=N_QUBITS)
     ap.add_argument("--skip-baselines", action="store_true", help="skip FP64/FP32 per-gate and CPU legs")
-    ap.add_argument("--profile-case", default=None, choices=["fused26"],
+    ap.add_argument("--profile-case", default=None, choices=["fused26", "trotter26"],
                     help="run a small fixed case for ncu captures instead of the benchmark")
     return ap.parse_args()
 
@@ -201,8 +201,9 @@ def trotter_leg(qi, workloads, stream, torch, np, rows=5, cols=6, steps=20, obse
     """First-order Trotter evolution on the 5x6 open lattice (30 qubits): anisotropic
     Heisenberg (1.0 XX + 0.8 YY + 0.5 ZZ per bond, h_i Z_i), 177 terms, dt = 0.05, from a
     seeded basis state.  The FP32 fused step (one plan per step, <H> every 10 steps) is
-    timed over `steps` steps; the FP64 step (one exp(-i c dt P) pass per term, the
-    reference's data flow) is timed over 2 steps, and <H> after 2 steps of both is compared."""
+    timed over `steps` steps; the FP64 step (grouped exponentials: one pass per run of
+    terms whose X-masks lie in {0, X}, i.e. one per bond plus the field run) is timed
+    over 2 steps, and <H> after 2 steps of both is compared."""
     n = rows * cols
     terms = workloads.lattice_xyz(rows, cols, seed=0)
     basis = int(np.random.default_rng(0).integers(0, 1 << n))
@@ -228,11 +229,11 @@ def trotter_leg(qi, workloads, stream, torch, np, rows=5, cols=6, steps=20, obse
     t64_step = (time.perf_counter() - t0) / 2
     e64_2 = qi.sumop_expectation(s64, terms).real
     s64.close()
-    out.update({"fp32_fused_ms_per_step": t32 * 1e3 / steps, "fp64_per_term_ms_per_step": t64_step * 1e3,
-                "speedup_fp32_fused_vs_fp64_per_term": t64_step / (t32 / steps),
+    out.update({"fp32_fused_ms_per_step": t32 * 1e3 / steps, "fp64_grouped_ms_per_step": t64_step * 1e3,
+                "speedup_fp32_fused_vs_fp64_grouped": t64_step / (t32 / steps),
                 "term_exponentials_per_s_fp32": len(terms) * steps / t32,
                 "energies_fp32_every_%d" % observe_every: [complex(e).real for e in e32],
-                "energy_after_2_steps_fp32_fused": e32_2, "energy_after_2_steps_fp64_per_term": e64_2,
+                "energy_after_2_steps_fp32_fused": e32_2, "energy_after_2_steps_fp64_grouped": e64_2,
                 "energy_error_fp32_2_steps": abs(e32_2 - e64_2),
                 "note": "FP32 timed region includes the <H> evaluations (every %d steps)" % observe_every})
     return out
@@ -298,6 +299,24 @@ def profile_case_fused26():
     print("profile case done, norm^2 = %.9f, <H> = %.9f" % (st.norm_sqr(), e))
 
 
+def profile_case_trotter26():
+    """Small case for ncu (26 qubits FP64 = 1 GB): two FP64 Trotter steps of the 2x13 lattice
+    anisotropic Heisenberg (76 terms) as grouped exponentials (k_pauli_group_pair,
+    k_pauli_group_diag), then the same two steps of an FP32 state (fused plan)."""
+    import __graft_entry__ as ge
+    qi = ge.load_package()
+    from quant_iron_gb300 import workloads
+    n = 26
+    terms = workloads.lattice_xyz(2, 13, seed=0)
+    for prec in (qi.F64, qi.F32):
+        st = qi.DeviceState(n, prec)
+        st.set_plus()
+        qi.trotter_evolve(st, terms, 0.05, 2)
+        st.synchronize()
+        print("profile case done, precision %d, norm^2 = %.9f" % (prec, st.norm_sqr()))
+        st.close()
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -305,6 +324,9 @@ def main():
         return
     if args.profile_case == "fused26":
         profile_case_fused26()
+        return
+    if args.profile_case == "trotter26":
+        profile_case_trotter26()
         return
     import numpy as np
     import torch

@@ -42,9 +42,22 @@ __global__ void __launch_bounds__(256) k_adjoint(typename Cx<T>::V2 *psi, typena
     V2 u[D * D];
 #pragma unroll
     for (int i = 0; i < D * D; ++i) u[i] = X::make((T)p.uinv[2 * i], (T)p.uinv[2 * i + 1]);
+    // dU/dtheta_k in the state's precision, converted once per block (conversions of the
+    // FP64 parameters inside the element loop would run on the FP64 pipe)
+    __shared__ V2 sd[3 * D * D];
+    for (int i = threadIdx.x; i < p.nd * D * D; i += blockDim.x)
+        sd[i] = X::make((T)p.d[i / (D * D)][2 * (i % (D * D))], (T)p.d[i / (D * D)][2 * (i % (D * D)) + 1]);
+    __syncthreads();
     double acc[3] = {0.0, 0.0, 0.0};
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t w = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; w < p.nwork; w += stride) {
+    // per-thread sums in T over kAdjBatch elements, folded into FP64 once per outer step
+    constexpr int kAdjBatch = 8;
+    for (uint64_t wb = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; wb < p.nwork; wb += stride * kAdjBatch) {
+      T part0 = 0, part1 = 0, part2 = 0;
+#pragma unroll 1
+      for (int bs = 0; bs < kAdjBatch; ++bs) {
+        const uint64_t w = wb + (uint64_t)bs * stride;
+        if (w >= p.nwork) break;
         const uint64_t base = insert_zeros(w, p.pos, p.np) | p.cmask;
         uint64_t idx[D];
         idx[0] = base;
@@ -76,17 +89,23 @@ __global__ void __launch_bounds__(256) k_adjoint(typename Cx<T>::V2 *psi, typena
             for (int r = 0; r < D; ++r) {
                 V2 dx = X::make(0, 0);
 #pragma unroll
-                for (int c = 0; c < D; ++c)
-                    dx = X::fma(X::make((T)p.d[k][2 * (r * D + c)], (T)p.d[k][2 * (r * D + c) + 1]), xn[c], dx);
+                for (int c = 0; c < D; ++c) dx = X::fma(sd[k * D * D + r * D + c], xn[c], dx);
                 re += l[r].x * dx.x + l[r].y * dx.y;   // Re(conj(lambda_r) * dx)
             }
-            acc[k] += (double)re;
+            // three named sums (a dynamically indexed array would live in local memory)
+            if (k == 0) part0 += re;
+            else if (k == 1) part1 += re;
+            else part2 += re;
         }
 #pragma unroll
         for (int r = 0; r < D; ++r) {
             psi[idx[r]] = xn[r];
             lam[idx[r]] = ln[r];
         }
+      }
+      acc[0] += (double)part0;
+      acc[1] += (double)part1;
+      acc[2] += (double)part2;
     }
     for (int k = 0; k < 3; ++k) {
         double v = block_sum(acc[k]);

@@ -116,20 +116,19 @@ __global__ void k_norm_partial(const typename Cx<T>::V2 *a, uint64_t dim, double
     if constexpr (sizeof(T) == 4) {
         const float4 *a4 = reinterpret_cast<const float4 *>(a);
         const uint64_t n4 = dim >> 1;
-        // FP32 sums of 8 float4 (16 amplitudes) folded into FP64: a conversion and an
-        // FP64 add per float4 would make this kernel FP64-bound on this part
-        float part = 0.0f;
-        int batch = 0;
-        for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n4; i += stride) {
-            float4 v = ldg_stream(a4 + i);
-            part += fmaf(v.x, v.x, fmaf(v.y, v.y, fmaf(v.z, v.z, v.w * v.w)));
-            if (++batch == 8) {
-                acc += (double)part;
-                part = 0.0f;
-                batch = 0;
-            }
+        // FP32 sums of 8 float4 (16 amplitudes) folded into FP64 once per outer step: a
+        // conversion and an FP64 add per float4 (or a fold the compiler if-converts into
+        // every iteration) make this kernel FP64-bound on this part
+        for (uint64_t i0 = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i0 < n4; i0 += 8 * stride) {
+            float4 v[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u)
+                v[u] = i0 + u * stride < n4 ? ldg_stream(a4 + i0 + u * stride) : make_float4(0.f, 0.f, 0.f, 0.f);
+            float part = 0.0f;
+#pragma unroll
+            for (int u = 0; u < 8; ++u) part += fmaf(v[u].x, v[u].x, fmaf(v[u].y, v[u].y, fmaf(v[u].z, v[u].z, v[u].w * v[u].w)));
+            acc += (double)part;
         }
-        acc += (double)part;
         if ((dim & 1) && blockIdx.x == 0 && threadIdx.x == 0) {   // dim == 1 only when n == 0
             float2 v = reinterpret_cast<const float2 *>(a)[dim - 1];
             acc += (double)v.x * v.x + (double)v.y * v.y;
@@ -154,10 +153,21 @@ __global__ void k_inner_partial(const typename Cx<T>::V2 *a, const typename Cx<T
         const float4 *a4 = reinterpret_cast<const float4 *>(a);
         const float4 *b4 = reinterpret_cast<const float4 *>(b);
         const uint64_t n4 = dim >> 1;
-        for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n4; i += stride) {
-            float4 x = ldg_stream(a4 + i), y = ldg_stream(b4 + i);
-            float r = fmaf(x.x, y.x, fmaf(x.y, y.y, fmaf(x.z, y.z, x.w * y.w)));
-            float m = fmaf(x.x, y.y, fmaf(-x.y, y.x, fmaf(x.z, y.w, -x.w * y.z)));
+        // FP32 sums of 4 float4 pairs (8 amplitudes) folded into FP64 once per outer step
+        for (uint64_t i0 = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i0 < n4; i0 += 4 * stride) {
+            float4 x[4], y[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const bool in = i0 + u * stride < n4;
+                x[u] = in ? ldg_stream(a4 + i0 + u * stride) : make_float4(0.f, 0.f, 0.f, 0.f);
+                y[u] = in ? ldg_stream(b4 + i0 + u * stride) : make_float4(0.f, 0.f, 0.f, 0.f);
+            }
+            float r = 0.0f, m = 0.0f;
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                r += fmaf(x[u].x, y[u].x, fmaf(x[u].y, y[u].y, fmaf(x[u].z, y[u].z, x[u].w * y[u].w)));
+                m += fmaf(x[u].x, y[u].y, fmaf(-x[u].y, y[u].x, fmaf(x[u].z, y[u].w, -x[u].w * y[u].z)));
+            }
             re += (double)r;
             im += (double)m;
         }

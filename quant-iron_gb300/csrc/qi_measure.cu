@@ -1,7 +1,8 @@
 // qi_measure.cu — State::measure / measure_n on the device.
 //
 // Reference: src/components/state.rs:525-784.  Probabilities of the measured
-// qubits are summed in FP64 on the device in a fixed order (one block per
+// qubits are summed in FP64 on the device in a fixed order (FP32 states: FP32
+// sums of 8 |a|^2, each folded into the FP64 sum; one block per
 // (outcome, chunk), then one ordered sum per outcome), copied to the host,
 // normalised and sampled exactly as the reference does (sequential CDF in
 // outcome order, `r < cumulative`, last outcome on fall-through).  The
@@ -37,10 +38,27 @@ __global__ void __launch_bounds__(256) k_meas_partial(const typename Cx<T>::V2 *
     for (int k = 0; k < g.nd; ++k) fixed |= ((d >> k) & 1ull) << g.pos[k];
     double acc = 0.0;
     const uint64_t lo = c * chunk, hi = min(rest_count, lo + chunk);
-    for (uint64_t w = lo + threadIdx.x; w < hi; w += blockDim.x) {
-        const uint64_t i = insert_zeros(w, g.pos, g.nd) | fixed;
-        const typename Cx<T>::V2 v = a[i];
-        acc += (double)v.x * (double)v.x + (double)v.y * (double)v.y;
+    if constexpr (sizeof(T) == 4) {
+        // FP32 |a|^2 summed over 8 amplitudes, folded into FP64 once per outer step
+        // (per-element FP64 arithmetic would bound this kernel on this part)
+        for (uint64_t w0 = lo + threadIdx.x; w0 < hi; w0 += 8 * (uint64_t)blockDim.x) {
+            float part = 0.0f;
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                const uint64_t w = w0 + (uint64_t)u * blockDim.x;
+                if (w < hi) {
+                    const float2 v = a[insert_zeros(w, g.pos, g.nd) | fixed];
+                    part += fmaf(v.x, v.x, v.y * v.y);
+                }
+            }
+            acc += (double)part;
+        }
+    } else {
+        for (uint64_t w = lo + threadIdx.x; w < hi; w += blockDim.x) {
+            const uint64_t i = insert_zeros(w, g.pos, g.nd) | fixed;
+            const typename Cx<T>::V2 v = a[i];
+            acc += v.x * v.x + v.y * v.y;
+        }
     }
     const double r = block_sum(acc);
     if (threadIdx.x == 0) partials[b] = r;

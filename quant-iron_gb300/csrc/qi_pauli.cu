@@ -636,9 +636,14 @@ __global__ void __launch_bounds__(256) k_diag_expect_f32(const float2 *a, int s,
     }
     const uint32_t iters = 1u << h;
     double dr = 0.0, di = 0.0;
-    float br = 0.0f, bi = 0.0f;
     constexpr int U = 2 * kExpUnroll;
-    for (uint32_t it0 = 0; it0 < iters; it0 += U) {
+    // FP32 sums of kExpBatch elements, folded into FP64 once per outer step (a fold
+    // inside the element loop may be if-converted into every iteration)
+    for (uint32_t b0 = 0; b0 < iters; b0 += kExpBatch) {
+      float br = 0.0f, bi = 0.0f;
+      const uint32_t bend = min(b0 + (uint32_t)kExpBatch, iters);
+#pragma unroll 1
+      for (uint32_t it0 = b0; it0 < bend; it0 += U) {
         float2 v[U];
 #pragma unroll
         for (int u = 0; u < U; ++u)
@@ -665,14 +670,10 @@ __global__ void __launch_bounds__(256) k_diag_expect_f32(const float2 *a, int s,
             br = fmaf(p, fr, br);
             bi = fmaf(p, fi, bi);
         }
-        if (((it0 / U) & (kExpBatch / U - 1)) == kExpBatch / U - 1) {
-            dr += br;
-            di += bi;
-            br = bi = 0.0f;
-        }
+      }
+      dr += br;
+      di += bi;
     }
-    dr += br;
-    di += bi;
     const double r0 = block_sum(dr), r1 = block_sum(di);
     if (threadIdx.x == 0) {
         partials[blockIdx.x * 4 + 0] = r0;
@@ -709,9 +710,14 @@ __global__ void __launch_bounds__(256) k_xgroup_expect_f32(const float2 *a, uint
     const IDX lo_mask = (IDX)((1ull << h) - 1), xm = (IDX)xmask;
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     double dr = 0.0, di = 0.0;
-    float br = 0.0f, bi = 0.0f;
-    int batch = 0;
-    for (uint64_t w0 = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; w0 < npairs; w0 += stride * kExpUnroll) {
+    // FP32 sums of kExpBatch pairs, folded into FP64 once per outer step (a fold inside
+    // the pair loop may be if-converted into every iteration)
+    for (uint64_t wb = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; wb < npairs; wb += stride * kExpBatch) {
+      float br = 0.0f, bi = 0.0f;
+#pragma unroll 1
+      for (int bstep = 0; bstep < kExpBatch / kExpUnroll; ++bstep) {
+        const uint64_t w0 = wb + (uint64_t)bstep * stride * kExpUnroll;
+        if (w0 >= npairs) break;
         float2 x[kExpUnroll], y[kExpUnroll];
         IDX iv[kExpUnroll];
 #pragma unroll
@@ -751,15 +757,10 @@ __global__ void __launch_bounds__(256) k_xgroup_expect_f32(const float2 *a, uint
             br += (fir * cr - fii * ci) + (fjr * cr + fji * ci);
             bi += (fir * ci + fii * cr) + (fji * cr - fjr * ci);
         }
-        if (++batch == kExpBatch / kExpUnroll) {
-            dr += br;
-            di += bi;
-            br = bi = 0.0f;
-            batch = 0;
-        }
+      }
+      dr += br;
+      di += bi;
     }
-    dr += br;
-    di += bi;
     const double r0 = block_sum(dr), r1 = block_sum(di);
     if (threadIdx.x == 0) {
         partials[blockIdx.x * 4 + 0] = r0;

@@ -10,7 +10,10 @@
 //   [D_re | D_im][m] += Im X[.][m] . [-Im U ; Re U ]^T     (imaginary half)
 // The B operands are the R x R blocks -Im U, Re U, Im U stored one after the
 // other along N (K-major, shared memory), so [Re U ; Im U] starts at block 1
-// and [-Im U ; Re U] at block 0.  Every operand is split as x = hi + lo with
+// and [-Im U ; Re U] at block 0.  Pair mode (below), short of shared memory,
+// keeps only Re U, Im U and splits the imaginary half into two N = R products,
+//   D_re -= Im X . Im U^T (negate-B)   and   D_im += Im X . Re U^T.
+// Every operand is split as x = hi + lo with
 // hi = tf32(x) (round to nearest) and lo = tf32(x - hi); the products
 // A_hi B_hi + A_hi B_lo + A_lo B_hi are accumulated in FP32, which keeps
 // about 22 significant bits (the dropped A_lo B_lo term is ~2^-22 relative).
@@ -25,8 +28,9 @@
 //     keeping the imaginary parts in registers; release the buffer
 //     (raw_empty[b]); split the imaginary parts into stage 1 once it is free;
 //     each stage is signalled on a_full[h]
-//   MMA issuer (1 thread): per half 3 products x R/8 MMAs (M128 x N2R x K8)
-//     into accumulator buffer it%2; tcgen05.commit frees the A stage
+//   MMA issuer (1 thread): per half 3 products x R/8 MMAs (M128 x N2R x K8;
+//     pair mode's imaginary half: two M128 x NR x K8 per step) into
+//     accumulator buffer it%2; tcgen05.commit frees the A stage
 //     (a_empty[h]) and publishes the accumulator (d_full[d])
 //   epilogue (4 warps): tcgen05.ld the accumulator, release it (d_empty[d]),
 //     store the amplitudes straight to global memory (rows r, r+1 as one
@@ -118,9 +122,9 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint
 }
 
 // Instruction descriptor, kind::tf32: D = F32, A = B = TF32, both K-major,
-// N >> 3 at bit 17, M >> 4 at bit 24.
-__host__ __device__ constexpr uint32_t tf32_idesc(uint32_t M, uint32_t N) {
-    return (1u << 4) | (2u << 7) | (2u << 10) | ((N >> 3) << 17) | ((M >> 4) << 24);
+// negate B at bit 14, N >> 3 at bit 17, M >> 4 at bit 24.
+__host__ __device__ constexpr uint32_t tf32_idesc(uint32_t M, uint32_t N, bool negate_b = false) {
+    return (1u << 4) | (2u << 7) | (2u << 10) | ((negate_b ? 1u : 0u) << 14) | ((N >> 3) << 17) | ((M >> 4) << 24);
 }
 
 __device__ __forceinline__ void mma_tf32_ts(uint32_t d_tmem, uint32_t a_tmem, uint64_t b_desc, uint32_t idesc,
@@ -247,21 +251,26 @@ __device__ __forceinline__ bool warp_wait_or_abort(uint64_t *bar, uint32_t parit
 }
 
 // ------------------------------------------------------------------ kernel
-template <int K>
+template <int K, bool PAIR = false>
 struct TcCfg {
     static constexpr int R = 1 << K;                   // rows (target patterns)
     static constexpr int BLK = R * R;                  // floats per operand block
     static constexpr uint32_t LBO = 128;               // next core matrix along K
     static constexpr uint32_t SBO = (R / 4) * 128;     // next 8-row group along N
-    static constexpr int NBUF = K == 6 ? 2 : 4;        // tile buffers in shared memory
+    // shared buffers: whole tiles, or (pair mode) a ring of units of 16 rows x 2 KB runs
+    static constexpr int NBUF = PAIR ? 5 : (K == 6 ? 2 : 6);
     static constexpr uint32_t STAGE = 2 * R;           // TMEM columns of one A stage or one accumulator
     static constexpr uint32_t COL_A = 0, COL_D = 2 * STAGE;
     static constexpr uint32_t TMEM_COLS = 4 * STAGE;   // 512 for k = 6, 256 for k = 5
     static constexpr int CONV_ROWS = R / 2;            // rows per converter thread (2 row slices)
     static constexpr int CHUNK = 16;                   // rows converted per step (register footprint)
     static constexpr uint32_t TILE_BYTES = (uint32_t)R * 128 * sizeof(float2);
-    static constexpr size_t OFF_TILES = 6 * (size_t)BLK * sizeof(float);
-    static constexpr size_t OFF_ROWX = OFF_TILES + (size_t)NBUF * TILE_BYTES;
+    static constexpr int UNIT_ROWS = 16;               // pair mode: rows per ring unit
+    static constexpr uint32_t BUF_BYTES = PAIR ? (uint32_t)UNIT_ROWS * 2 * 128 * sizeof(float2) : TILE_BYTES;
+    // operand blocks in shared memory: -Im U, Re U, Im U (hi, then lo); pair mode Re U, Im U
+    static constexpr int NBLK = PAIR ? 4 : 6;
+    static constexpr size_t OFF_TILES = (size_t)NBLK * BLK * sizeof(float);
+    static constexpr size_t OFF_ROWX = OFF_TILES + (size_t)NBUF * BUF_BYTES;
     static constexpr size_t OFF_GROW = OFF_ROWX + 64 * sizeof(uint32_t);
     static constexpr size_t OFF_BAR = OFF_GROW + 64 * sizeof(uint64_t);
     static constexpr int NBARS = 2 * NBUF + 9;
@@ -301,19 +310,20 @@ __device__ __forceinline__ void split_store(uint32_t taddr_hi, uint32_t taddr_lo
     tmem_st<N>(taddr_lo, v);
 }
 
-// PAIR: a CTA takes tiles in pairs (2p, 2p+1), which differ in qubit L, so the row
+// PAIR: a CTA takes tiles in pairs (2p, 2p+1), which differ in qubit L = 7, so the row
 // runs of the two tiles are adjacent in memory; one bulk copy of 2 x 2^L amplitudes per
-// row run loads both.  The two shared buffers then hold the pair's row halves (top
-// target bit 0 / 1), read by converter slice 0 / 1, and are released after the pair's
-// second tile.  Used when the runs are short (1-2 KB), where the copy granularity bounds
-// the load rate.
+// row run loads both.  The pair's rows go through a ring of NBUF units of 16 rows
+// (unit u = 2c + s: chunk c of converter slice s); a unit is released after the pair's
+// second tile has read it, so the next pair's first units load while the second tile
+// is converted.  Used when the runs are 1 KB (all targets above qubit 7), where the
+// copy granularity bounds the load rate.
 template <int K, bool PAIR>
 __global__ void __launch_bounds__(kTcThreads, 1) k_fused_tc(float2 *a, const float *blocks, TileGeom g, int *err_flag) {
-    using C = TcCfg<K>;
+    using C = TcCfg<K, PAIR>;
     constexpr int R = C::R, NB = C::NBUF;
-    static_assert(!PAIR || NB == 2, "pair mode uses one buffer per converter slice");
+    static_assert(!PAIR || (K == 6 && C::UNIT_ROWS == C::CHUNK), "pair mode: K = 6, one ring unit per chunk");
     extern __shared__ __align__(1024) unsigned char smem_raw[];
-    float *sB = reinterpret_cast<float *>(smem_raw);   // 6 operand blocks: -Im, Re, Im (hi), then (lo)
+    float *sB = reinterpret_cast<float *>(smem_raw);   // operand blocks (C::NBLK)
     unsigned char *tiles = smem_raw + C::OFF_TILES;
     uint32_t *rowx = reinterpret_cast<uint32_t *>(smem_raw + C::OFF_ROWX);
     uint64_t *grow = reinterpret_cast<uint64_t *>(smem_raw + C::OFF_GROW);
@@ -325,11 +335,17 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_fused_tc(float2 *a, const flo
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
-    // operand blocks -> shared memory (16-byte vectors), visible to the async proxy
+    // operand blocks -> shared memory (16-byte vectors), visible to the async proxy;
+    // pair mode takes blocks 1, 2, 4, 5 (Re U, Im U; hi then lo) of the six
     {
         const uint4 *src = reinterpret_cast<const uint4 *>(blocks);
         uint4 *dst = reinterpret_cast<uint4 *>(sB);
-        for (int i = tid; i < (int)(C::OFF_TILES / 16); i += kTcThreads) dst[i] = src[i];
+        constexpr int per_blk = C::BLK * (int)sizeof(float) / 16;
+        for (int i = tid; i < C::NBLK * per_blk; i += kTcThreads) {
+            const int blk = i / per_blk;
+            const int from = PAIR ? (blk < 2 ? blk + 1 : blk + 2) : blk;
+            dst[i] = src[from * per_blk + i % per_blk];
+        }
     }
     asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
     // row r (bit j <-> target j) -> tile-local position and global offset
@@ -343,9 +359,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_fused_tc(float2 *a, const flo
         }
         for (int j = 0; j < g.nhigh; ++j) {
             const uint32_t bit = ((uint32_t)tid >> (g.nlow_t + j)) & 1u;
-            // pair mode: the top high target selects the buffer; the others index runs of 2 x 2^L
+            // pair mode: the two top row bits select the ring unit; the others index its runs of 2 x 2^L
             if (!PAIR) x |= bit << (g.L + j);
-            else if (j < g.nhigh - 1) x |= bit << (g.L + 1 + j);
+            else if (j < g.nhigh - 2) x |= bit << (g.L + 1 + j);
             go |= (uint64_t)bit << g.high_t[j];
         }
         rowx[tid] = x;
@@ -354,7 +370,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_fused_tc(float2 *a, const flo
     if (tid == 0) {
         for (int i = 0; i < NB; ++i) {
             mbar_init(raw_full + i, 1);
-            mbar_init(raw_empty + i, PAIR ? kConvWarps / 2 : kConvWarps);
+            mbar_init(raw_empty + i, PAIR ? kConvWarps / 2 : kConvWarps);   // pair mode: one slice per unit
         }
         for (int i = 0; i < 2; ++i) {
             mbar_init(a_full + i, kConvWarps);
@@ -387,19 +403,29 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_fused_tc(float2 *a, const flo
         const uint32_t lane_base = (uint32_t)(quarter * 32) << 16;
         const int r0 = slice * C::CONV_ROWS;
         for (int it = 0; tile_of(it) < ntiles; ++it) {
-            const int b = PAIR ? slice : it % NB;
-            const bool first = !PAIR || (it & 1) == 0;   // pair mode: the pair's 2nd tile reuses the buffer
-            const uint32_t ph = PAIR ? (uint32_t)(it >> 1) & 1u : (uint32_t)(it / NB) & 1u;
-            if (first && !warp_wait_or_abort(raw_full + b, ph, abort_flag, err_flag)) break;
-            const float2 *S = reinterpret_cast<const float2 *>(tiles + (size_t)b * C::TILE_BYTES) +
-                              (PAIR ? ((uint32_t)(it & 1) << g.L) : 0u);
+            const int b = it % NB;   // whole-tile buffer (pair mode: units, below)
+            if (!PAIR && !warp_wait_or_abort(raw_full + b, (uint32_t)(it / NB) & 1u, abort_flag, err_flag)) break;
             // real half -> A stage 0, once the products of the previous tile have read it;
             // the imaginary parts stay in registers for stage 1
             if (it > 0 && !warp_wait_or_abort(a_empty + 0, (uint32_t)(it - 1) & 1u, abort_flag, err_flag)) break;
             tc_fence_after();
+            bool ok = true;
             float im[C::CONV_ROWS];
 #pragma unroll
             for (int c0 = 0; c0 < C::CONV_ROWS; c0 += C::CHUNK) {
+                const float2 *S;
+                uint32_t unit = 0;
+                if constexpr (PAIR) {
+                    const uint32_t k = 4u * (uint32_t)(it >> 1) + 2u * (uint32_t)(c0 / C::CHUNK) + (uint32_t)slice;
+                    unit = k % NB;
+                    if (!(it & 1) && !warp_wait_or_abort(raw_full + unit, (k / NB) & 1u, abort_flag, err_flag)) {
+                        ok = false;
+                        break;
+                    }
+                    S = reinterpret_cast<const float2 *>(tiles + (size_t)unit * C::BUF_BYTES) + ((uint32_t)(it & 1) << g.L);
+                } else {
+                    S = reinterpret_cast<const float2 *>(tiles + (size_t)b * C::BUF_BYTES);
+                }
                 float re[C::CHUNK];
                 if (pair_rows) {
 #pragma unroll
@@ -420,9 +446,16 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_fused_tc(float2 *a, const flo
                 }
                 split_store<C::CHUNK>(tmem + lane_base + C::COL_A + r0 + c0, tmem + lane_base + C::COL_A + R + r0 + c0,
                                       re);
+                if constexpr (PAIR) {   // the pair's second tile was the unit's last reader
+                    __syncwarp();
+                    if (lane == 0 && (it & 1)) mbar_arrive(raw_empty + unit);
+                }
             }
-            __syncwarp();
-            if (lane == 0 && (!PAIR || (it & 1))) mbar_arrive(raw_empty + b);   // the buffer may take the next tile
+            if (!ok) break;
+            if (!PAIR) {
+                __syncwarp();
+                if (lane == 0) mbar_arrive(raw_empty + b);   // the buffer may take the next tile
+            }
             tmem_wait_st();
             tc_fence_before();
             __syncwarp();
@@ -498,29 +531,31 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_fused_tc(float2 *a, const flo
                 for (int j = issued > NB ? issued - NB : 0; j < issued; ++j)
                     if (!mbar_wait_bounded(raw_full + (j % NB), (uint32_t)(j / NB) & 1u)) atomicExch(err_flag, 2);
             } else {
-                // buffer s <- the pair's rows with top target bit s: runs of 2 x 2^L amplitudes
-                const int half_runs = 1 << (g.nhigh - 1);
-                int issued[2] = {0, 0};
+                // ring unit k (pair k / 4, u = k % 4 = 2c + s) <- rows 32 s + 16 c .. + 15 of the
+                // pair: runs of 2 x 2^L amplitudes (both tiles), in the order the converters use them
+                int issued = 0;
                 bool ok = true;
-                for (int ip = 0; ok && tile_of(2 * ip) < ntiles; ++ip) {
-                    const uint64_t base = tile_base(g, tile_of(2 * ip));
-                    for (int s = 0; s < 2; ++s) {
-                        if (ip >= 1 && !wait_or_abort(raw_empty + s, (uint32_t)(ip - 1) & 1u, abort_flag, err_flag)) {
+                for (uint32_t lp = 0; ok && tile_of(2 * (int)lp) < ntiles; ++lp) {
+                    const uint64_t base = tile_base(g, tile_of(2 * (int)lp));
+                    for (uint32_t u = 0; u < 4; ++u) {
+                        const uint32_t k = 4 * lp + u, unit = k % NB;
+                        if (k >= (uint32_t)NB &&
+                            !wait_or_abort(raw_empty + unit, (k / NB - 1) & 1u, abort_flag, err_flag)) {
                             ok = false;
                             break;
                         }
-                        mbar_arrive_expect_tx(raw_full + s, C::TILE_BYTES);
-                        unsigned char *dst = tiles + (size_t)s * C::TILE_BYTES;
-                        for (int h = 0; h < half_runs; ++h)
-                            bulk_load(dst + (size_t)h * 2 * run_bytes,
-                                      a + (base | grow[(h | (s << (g.nhigh - 1))) << g.nlow_t]), 2 * run_bytes,
-                                      raw_full + s);
-                        issued[s] = ip + 1;
+                        mbar_arrive_expect_tx(raw_full + unit, C::BUF_BYTES);
+                        unsigned char *dst = tiles + (size_t)unit * C::BUF_BYTES;
+                        const int row0 = 32 * (int)(u & 1u) + C::UNIT_ROWS * (int)(u >> 1);
+                        for (int i = 0; i < C::UNIT_ROWS; ++i)
+                            bulk_load(dst + (size_t)i * 2 * run_bytes, a + (base | grow[row0 + i]), 2 * run_bytes,
+                                      raw_full + unit);
+                        issued = (int)k + 1;
                     }
                 }
-                for (int s = 0; s < 2; ++s)
-                    if (issued[s] > 0 && !mbar_wait_bounded(raw_full + s, (uint32_t)(issued[s] - 1) & 1u))
-                        atomicExch(err_flag, 2);
+                // copies still in flight (only after an abort) land before the CTA exits
+                for (int j = issued > NB ? issued - NB : 0; j < issued; ++j)
+                    if (!mbar_wait_bounded(raw_full + (j % NB), (uint32_t)(j / NB) & 1u)) atomicExch(err_flag, 2);
             }
         }
         __syncwarp();
@@ -530,7 +565,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_fused_tc(float2 *a, const flo
             // Descriptor of block 0 at K offset 0; every MMA adds a constant byte offset
             // (>> 4 into the start-address field, which cannot carry: blocks stay below 256 KB).
             const uint64_t desc0 = smem_desc(smem_u32(sB), C::LBO, C::SBO);
-            constexpr uint32_t idesc = tf32_idesc(128, 2 * R);
+            constexpr uint32_t idesc = tf32_idesc(128, 2 * R), idesc_r = tf32_idesc(128, R),
+                               idesc_rneg = tf32_idesc(128, R, true);
             bool ok = true;
             for (int it = 0; ok && tile_of(it) < ntiles; ++it) {
                 const int d = it & 1;
@@ -548,12 +584,24 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_fused_tc(float2 *a, const flo
                     const uint32_t acol = tmem + C::COL_A + h * C::STAGE;
 #pragma unroll
                     for (int p = 0; p < 3; ++p) {   // (A_hi, B_hi), (A_hi, B_lo), (A_lo, B_hi)
-                        const int blk = (p == 1 ? 3 : 0) + (h == 0 ? 1 : 0);
 #pragma unroll
                         for (int j = 0; j < R / 8; ++j) {
-                            const uint32_t boff = (uint32_t)(blk * C::BLK * 4) + (uint32_t)(2 * j) * C::LBO;
-                            mma_tf32_ts(dcol, acol + (p == 2 ? R : 0) + 8 * j, desc0 + (uint64_t)(boff >> 4), idesc,
-                                        (h | p | j) ? 1u : 0u);
+                            const uint32_t kstep = (uint32_t)(2 * j) * C::LBO;
+                            const uint32_t a_col = acol + (p == 2 ? R : 0) + 8 * j;
+                            if constexpr (!PAIR) {   // window [Re U ; Im U] (block 1) or [-Im U ; Re U] (block 0)
+                                const int blk = (p == 1 ? 3 : 0) + (h == 0 ? 1 : 0);
+                                const uint32_t boff = (uint32_t)(blk * C::BLK * 4) + kstep;
+                                mma_tf32_ts(dcol, a_col, desc0 + (uint64_t)(boff >> 4), idesc, (h | p | j) ? 1u : 0u);
+                            } else {
+                                const int blk = p == 1 ? 2 : 0;   // Re U of the hi or lo pair, Im U next to it
+                                const uint32_t b_re = (uint32_t)(blk * C::BLK * 4) + kstep, b_im = b_re + C::BLK * 4;
+                                if (h == 0) {   // [D_re | D_im] += Re X . [Re U ; Im U]^T
+                                    mma_tf32_ts(dcol, a_col, desc0 + (uint64_t)(b_re >> 4), idesc, (p | j) ? 1u : 0u);
+                                } else {        // D_re -= Im X . Im U^T;  D_im += Im X . Re U^T
+                                    mma_tf32_ts(dcol, a_col, desc0 + (uint64_t)(b_im >> 4), idesc_rneg, 1u);
+                                    mma_tf32_ts(dcol + R, a_col, desc0 + (uint64_t)(b_re >> 4), idesc_r, 1u);
+                                }
+                            }
                         }
                     }
                     mma_commit(a_empty + h);
@@ -609,7 +657,7 @@ void tc_blocks(int k, const double *U, std::vector<float> &out) {
 
 template <int K, bool PAIR>
 static Status launch_tc_t(qi_state *s, const TileGeom &g, const void *d_tc) {
-    using C = TcCfg<K>;
+    using C = TcCfg<K, PAIR>;
     static_assert(C::SMEM <= 232448, "shared memory per CTA");
     static bool attr_set = false;
     static int num_sms = 0;
@@ -638,7 +686,7 @@ Status launch_fused_tc(qi_state *s, int k, const int32_t *targets, const void *d
     // Tile pairs when a tile's rows are 1 KB runs (all targets at qubit 7 or above): tiles 2p,
     // 2p + 1 differ in qubit L = 7, so each pair of runs is one 2 KB copy.  (Measured: 1 KB runs
     // gain ~8 %; with 2 KB runs the pair's longer buffer occupancy costs more than it saves.)
-    const bool pair = k == 6 && g.nhigh >= 1 && g.nfree >= 1 && g.L == 7 && g.L < n;
+    const bool pair = k == 6 && g.nlow_t == 0 && g.nhigh == 6 && g.nfree >= 1 && g.L == 7 && g.L < n;
     if (k == 5) return launch_tc_t<5, false>(s, g, d_tc);
     return pair ? launch_tc_t<6, true>(s, g, d_tc) : launch_tc_t<6, false>(s, g, d_tc);
 }

@@ -343,7 +343,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_fused_tc(float2 *a, const flo
         constexpr int per_blk = C::BLK * (int)sizeof(float) / 16;
         for (int i = tid; i < C::NBLK * per_blk; i += kTcThreads) {
             const int blk = i / per_blk;
-            const int from = PAIR ? (blk < 2 ? blk + 1 : blk + 2) : blk;
+            const int from = C::NBLK == 4 ? (blk < 2 ? blk + 1 : blk + 2) : blk;
             dst[i] = src[from * per_blk + i % per_blk];
         }
     }
@@ -683,9 +683,10 @@ Status launch_fused_tc(qi_state *s, int k, const int32_t *targets, const void *d
     const TileGeom g = make_tile_geom(n, k, targets, 7);
     if (g.nfree != n - k - 7) return err(QI_ERR_UNKNOWN, g.nfree, n - k - 7, "tile decomposition");
     if (((uintptr_t)d_tc & 15) != 0) return err(QI_ERR_UNKNOWN, -1, -1, "operand blocks must be 16-byte aligned");
-    // Tile pairs when a tile's rows are 1 KB runs (all targets at qubit 7 or above): tiles 2p,
-    // 2p + 1 differ in qubit L = 7, so each pair of runs is one 2 KB copy.  (Measured: 1 KB runs
-    // gain ~8 %; with 2 KB runs the pair's longer buffer occupancy costs more than it saves.)
+    // Tile pairs when a tile's rows are 1 KB runs (all targets above qubit 7): tiles 2p, 2p + 1
+    // differ in qubit L = 7, so each pair of runs is one 2 KB copy.  (Measured at 30 qubits: 3.28 ms
+    // per launch against 4.4 ms for single tiles of 1 KB runs; a 4-unit ring with the N = 2R
+    // imaginary half took 3.83 ms, so the ring depth matters more than the extra MMAs.)
     const bool pair = k == 6 && g.nlow_t == 0 && g.nhigh == 6 && g.nfree >= 1 && g.L == 7 && g.L < n;
     if (k == 5) return launch_tc_t<5, false>(s, g, d_tc);
     return pair ? launch_tc_t<6, true>(s, g, d_tc) : launch_tc_t<6, false>(s, g, d_tc);

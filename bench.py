@@ -418,6 +418,14 @@ def main():
                 "kernels": {k: {"launches": v["launches"], "ms": round(v["ms"], 3),
                                 "share": round(v["ms"] / max(1e-9, sum(x["ms"] for x in by_kernel.values())), 4)}
                             for k, v in by_kernel.items()}}
+    if dom == "k_fused_tc":
+        # the same kernel against the tensor roof: 3 split products x 8 * 2^k flop per amplitude
+        # (k = 6: 1536 flop/amp) per launch; peak = the nominal dense TF32 rate (no measured TF32
+        # figure exists for this pool), so the fraction is of nominal
+        tflop = 3 * 8 * (1 << FUSED_K) * (1 << n) / 1e12
+        roofline["tensor"] = {"achieved": tflop / (avg_ms / 1e3), "peak": 1100.0, "unit": "TFLOP/s",
+                              "frac": tflop / (avg_ms / 1e3) / 1100.0, "peak_source": "nominal dense TF32",
+                              "flop_per_amp": 3 * 8 * (1 << FUSED_K)}
 
     # energy of the final state (FP64 reduction), and the time of SumOp::expectation_value
     energy = qi.sumop_expectation(st, terms).real

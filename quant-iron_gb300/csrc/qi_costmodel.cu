@@ -1,9 +1,9 @@
 // qi_costmodel.cu — partition choice for the fusion pass, and the engine's
 // own timing collection that trains the learned cost model (qi_mlp.cu).
 //
-// QI_FUSION_GREEDY uses the greedy fixed-k fuser.  QI_FUSION_LEARNED builds
-// the candidate partitions {one kernel per gate} and {greedy k, tensor cores
-// on/off} for k = 2..kmax, predicts every device op's time with the trained
+// QI_FUSION_GREEDY uses the greedy fixed-k fuser (window_partition, qi_plan.cu).
+// QI_FUSION_LEARNED builds the candidate partitions {one kernel per gate} and
+// {greedy k, tensor cores on/off} for k = 2..kmax, predicts every device op's time with the trained
 // MLP, and keeps the candidate with the smallest predicted sum; without a
 // trained model it falls back to greedy.
 #include "qi_plan.hpp"
@@ -17,7 +17,7 @@
 namespace qi {
 
 std::vector<Block> choose_partition(qi_plan *p, const std::vector<Elem> &elems, int kmax) {
-    return greedy_partition(elems, p->n, kmax);
+    return window_partition(elems, p->n, kmax);
 }
 
 // Features of the device ops one candidate produces.
@@ -46,7 +46,7 @@ static void candidate_features(int n, bool f32, const std::vector<Elem> &elems, 
         for (const Elem &e : elems) add_single(e);
         return;
     }
-    std::vector<Block> blocks = greedy_partition(elems, n, k);
+    std::vector<Block> blocks = window_partition(elems, n, k);
     bool used_tc = false;
     for (const Block &b : blocks) {
         if (b.single) { add_single(elems[b.members[0]]); continue; }

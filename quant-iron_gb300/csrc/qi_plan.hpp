@@ -25,6 +25,10 @@ struct Block {
 };
 
 std::vector<Block> greedy_partition(const std::vector<Elem> &elems, int n, int kmax);
+// Greedy over candidate blocks: the light-cone block of the first remaining element
+// (taken as is when it is all-diagonal), and everything each window of kmax
+// consecutive qubits can absorb; the candidate with the most elements wins.
+std::vector<Block> window_partition(const std::vector<Elem> &elems, int n, int kmax);
 void compose_block(const std::vector<Elem> &elems, const Block &b, std::vector<int> &qubits,
                    std::vector<std::complex<double>> &B);
 

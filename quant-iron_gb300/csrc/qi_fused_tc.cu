@@ -310,6 +310,29 @@ __device__ __forceinline__ void split_store(uint32_t taddr_hi, uint32_t taddr_lo
     tmem_st<N>(taddr_lo, v);
 }
 
+// out[p] = a[(p - s) mod 8]: undoes a per-lane rotation of 8 values (s in 0..7),
+// three select stages with compile-time indices.
+__device__ __forceinline__ void unrotate8(float (&a)[8], int s) {
+#pragma unroll
+    for (int st = 0; st < 3; ++st) {
+        const int k = 1 << st;
+        const bool on = (s >> st) & 1;
+        float t[8];
+#pragma unroll
+        for (int p = 0; p < 8; ++p) t[p] = on ? a[(p - k) & 7] : a[p];
+#pragma unroll
+        for (int p = 0; p < 8; ++p) a[p] = t[p];
+    }
+}
+
+// 32-byte streaming store of four consecutive amplitudes (address 32-byte aligned).
+__device__ __forceinline__ void st_cs_v8(float2 *p, float a0, float a1, float a2, float a3, float a4, float a5,
+                                         float a6, float a7) {
+    asm volatile("st.global.cs.v8.f32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};\n" ::"l"(p), "f"(a0), "f"(a1),
+                 "f"(a2), "f"(a3), "f"(a4), "f"(a5), "f"(a6), "f"(a7)
+                 : "memory");
+}
+
 // PAIR: a CTA takes tiles in pairs (2p, 2p+1), which differ in qubit L = 7, so the row
 // runs of the two tiles are adjacent in memory; one bulk copy of 2 x 2^L amplitudes per
 // row run loads both.  The pair's rows go through a ring of NBUF units of 16 rows
@@ -317,11 +340,15 @@ __device__ __forceinline__ void split_store(uint32_t taddr_hi, uint32_t taddr_lo
 // second tile has read it, so the next pair's first units load while the second tile
 // is converted.  Used when the runs are 1 KB (all targets above qubit 7), where the
 // copy granularity bounds the load rate.
-template <int K, bool PAIR>
+// ROT: qubits 0-3 are all targets, so the tile's columns are 128 bytes or more apart and the
+// 8 lanes of a quarter warp would read the same banks for one row pair; each lane then reads the
+// chunk's row pairs starting at its own (lane mod 8), undone in registers.
+template <int K, bool PAIR, bool ROT>
 __global__ void __launch_bounds__(kTcThreads, 1) k_fused_tc(float2 *a, const float *blocks, TileGeom g, int *err_flag) {
     using C = TcCfg<K, PAIR>;
     constexpr int R = C::R, NB = C::NBUF;
     static_assert(!PAIR || (K == 6 && C::UNIT_ROWS == C::CHUNK), "pair mode: K = 6, one ring unit per chunk");
+    static_assert(!(PAIR && ROT), "pair-mode tiles have qubit 0 as a column");
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     float *sB = reinterpret_cast<float *>(smem_raw);   // operand blocks (C::NBLK)
     unsigned char *tiles = smem_raw + C::OFF_TILES;
@@ -395,6 +422,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_fused_tc(float2 *a, const flo
                     : blockIdx.x + (uint32_t)it * gridDim.x;
     };
     const bool pair_rows = !g.q0_is_col;   // qubit 0 is target 0: rows r, r+1 are adjacent amplitudes
+    // qubits 0 and 1 both targets: rows r..r+3 are four adjacent amplitudes (one 32-byte store)
+    const bool quad_rows = pair_rows && g.nlow_t >= 2 && g.low_t[1] == 1;
 
     if (warp < kConvWarps) {
         // ------------------------------------------------ converters
@@ -427,7 +456,32 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_fused_tc(float2 *a, const flo
                     S = reinterpret_cast<const float2 *>(tiles + (size_t)b * C::BUF_BYTES);
                 }
                 float re[C::CHUNK];
-                if (pair_rows) {
+                if constexpr (ROT) {
+                    static_assert(C::CHUNK == 16, "8 row pairs per chunk");
+                    // lane reads row pair (j + lane) mod 8 at step j: 8 lanes, 8 bank groups
+                    const int sft = lane & 7;
+                    float r0v[8], i0v[8], r1v[8], i1v[8];
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) {
+                        const int pr = (j + sft) & 7;
+                        const float4 v = *reinterpret_cast<const float4 *>(S + (rowx[r0 + c0 + 2 * pr] | cx));
+                        r0v[j] = v.x;
+                        i0v[j] = v.y;
+                        r1v[j] = v.z;
+                        i1v[j] = v.w;
+                    }
+                    unrotate8(r0v, sft);
+                    unrotate8(i0v, sft);
+                    unrotate8(r1v, sft);
+                    unrotate8(i1v, sft);
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) {
+                        re[2 * j] = r0v[j];
+                        im[c0 + 2 * j] = i0v[j];
+                        re[2 * j + 1] = r1v[j];
+                        im[c0 + 2 * j + 1] = i1v[j];
+                    }
+                } else if (pair_rows) {
 #pragma unroll
                     for (int i = 0; i < C::CHUNK; i += 2) {
                         const float4 v = *reinterpret_cast<const float4 *>(S + (rowx[r0 + c0 + i] | cx));
@@ -496,7 +550,13 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_fused_tc(float2 *a, const flo
                     __syncwarp();
                     if (lane == 0) mbar_arrive(d_empty + d);
                 }
-                if (pair_rows) {
+                if (quad_rows) {
+#pragma unroll
+                    for (int i = 0; i < 16; i += 4)
+                        st_cs_v8(out + grow[16 * c + i], __uint_as_float(vr[i]), __uint_as_float(vi[i]),
+                                 __uint_as_float(vr[i + 1]), __uint_as_float(vi[i + 1]), __uint_as_float(vr[i + 2]),
+                                 __uint_as_float(vi[i + 2]), __uint_as_float(vr[i + 3]), __uint_as_float(vi[i + 3]));
+                } else if (pair_rows) {
 #pragma unroll
                     for (int i = 0; i < 16; i += 2)
                         __stcs(reinterpret_cast<float4 *>(out + grow[16 * c + i]),
@@ -655,14 +715,14 @@ void tc_blocks(int k, const double *U, std::vector<float> &out) {
     }
 }
 
-template <int K, bool PAIR>
+template <int K, bool PAIR, bool ROT>
 static Status launch_tc_t(qi_state *s, const TileGeom &g, const void *d_tc) {
     using C = TcCfg<K, PAIR>;
     static_assert(C::SMEM <= 232448, "shared memory per CTA");
     static bool attr_set = false;
     static int num_sms = 0;
     if (!attr_set) {
-        QI_CUDA(cudaFuncSetAttribute(k_fused_tc<K, PAIR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::SMEM));
+        QI_CUDA(cudaFuncSetAttribute(k_fused_tc<K, PAIR, ROT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::SMEM));
         int dev = 0;
         QI_CUDA(cudaGetDevice(&dev));
         QI_CUDA(cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, dev));
@@ -670,7 +730,7 @@ static Status launch_tc_t(qi_state *s, const TileGeom &g, const void *d_tc) {
     }
     uint64_t grid = PAIR ? g.ntiles / 2 : g.ntiles;   // one persistent CTA per SM
     if (grid > (uint64_t)num_sms) grid = (uint64_t)num_sms;
-    k_fused_tc<K, PAIR><<<(unsigned)grid, kTcThreads, C::SMEM, s->stream>>>((float2 *)s->amps, (const float *)d_tc,
+    k_fused_tc<K, PAIR, ROT><<<(unsigned)grid, kTcThreads, C::SMEM, s->stream>>>((float2 *)s->amps, (const float *)d_tc,
                                                                             g, s->d_flag);
     count_launch();
     return check_launch("k_fused_tc");
@@ -688,8 +748,12 @@ Status launch_fused_tc(qi_state *s, int k, const int32_t *targets, const void *d
     // per launch against 4.4 ms for single tiles of 1 KB runs; a 4-unit ring with the N = 2R
     // imaginary half took 3.83 ms, so the ring depth matters more than the extra MMAs.)
     const bool pair = k == 6 && g.nlow_t == 0 && g.nhigh == 6 && g.nfree >= 1 && g.L == 7 && g.L < n;
-    if (k == 5) return launch_tc_t<5, false>(s, g, d_tc);
-    return pair ? launch_tc_t<6, true>(s, g, d_tc) : launch_tc_t<6, false>(s, g, d_tc);
+    // qubits 0-3 all targets: lane-rotated row reads (k_fused_tc's ROT)
+    bool rot = true;
+    for (int q = 0; q < 4; ++q) rot = rot && std::find(targets, targets + k, q) != targets + k;
+    if (k == 5) return rot ? launch_tc_t<5, false, true>(s, g, d_tc) : launch_tc_t<5, false, false>(s, g, d_tc);
+    if (pair) return launch_tc_t<6, true, false>(s, g, d_tc);
+    return rot ? launch_tc_t<6, false, true>(s, g, d_tc) : launch_tc_t<6, false, false>(s, g, d_tc);
 }
 
 }  // namespace qi

@@ -258,14 +258,15 @@ struct TcCfg {
     static constexpr uint32_t LBO = 128;               // next core matrix along K
     static constexpr uint32_t SBO = (R / 4) * 128;     // next 8-row group along N
     // shared buffers: whole tiles, or (pair mode) a ring of units of 16 rows x 2 KB runs
-    static constexpr int NBUF = PAIR ? 5 : (K == 6 ? 2 : 6);
+    static constexpr int NBUF = PAIR ? 10 : (K == 6 ? 2 : 6);
     static constexpr uint32_t STAGE = 2 * R;           // TMEM columns of one A stage or one accumulator
     static constexpr uint32_t COL_A = 0, COL_D = 2 * STAGE;
     static constexpr uint32_t TMEM_COLS = 4 * STAGE;   // 512 for k = 6, 256 for k = 5
     static constexpr int CONV_ROWS = R / 2;            // rows per converter thread (2 row slices)
-    static constexpr int CHUNK = 16;                   // rows converted per step (register footprint)
+    static constexpr int CHUNK = PAIR ? 8 : 16;        // rows converted per step (register footprint)
     static constexpr uint32_t TILE_BYTES = (uint32_t)R * 128 * sizeof(float2);
-    static constexpr int UNIT_ROWS = 16;               // pair mode: rows per ring unit
+    static constexpr int UNIT_ROWS = 8;                // pair mode: rows per ring unit (one chunk)
+    static constexpr int UNITS_PER_PAIR = 2 * CONV_ROWS / UNIT_ROWS;   // pair mode: 8
     static constexpr uint32_t BUF_BYTES = PAIR ? (uint32_t)UNIT_ROWS * 2 * 128 * sizeof(float2) : TILE_BYTES;
     // operand blocks in shared memory: -Im U, Re U, Im U (hi, then lo); pair mode Re U, Im U
     static constexpr int NBLK = PAIR ? 4 : 6;
@@ -335,7 +336,7 @@ __device__ __forceinline__ void st_cs_v8(float2 *p, float a0, float a1, float a2
 
 // PAIR: a CTA takes tiles in pairs (2p, 2p+1), which differ in qubit L = 7, so the row
 // runs of the two tiles are adjacent in memory; one bulk copy of 2 x 2^L amplitudes per
-// row run loads both.  The pair's rows go through a ring of NBUF units of 16 rows
+// row run loads both.  The pair's rows go through a ring of NBUF units of 8 rows
 // (unit u = 2c + s: chunk c of converter slice s); a unit is released after the pair's
 // second tile has read it, so the next pair's first units load while the second tile
 // is converted.  Used when the runs are 1 KB (all targets above qubit 7), where the
@@ -386,9 +387,10 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_fused_tc(float2 *a, const flo
         }
         for (int j = 0; j < g.nhigh; ++j) {
             const uint32_t bit = ((uint32_t)tid >> (g.nlow_t + j)) & 1u;
-            // pair mode: the two top row bits select the ring unit; the others index its runs of 2 x 2^L
+            // pair mode: the top row bits select the ring unit (slice, chunk); the others index
+            // its runs of 2 x 2^L
             if (!PAIR) x |= bit << (g.L + j);
-            else if (j < g.nhigh - 2) x |= bit << (g.L + 1 + j);
+            else if ((1 << j) < C::UNIT_ROWS) x |= bit << (g.L + 1 + j);
             go |= (uint64_t)bit << g.high_t[j];
         }
         rowx[tid] = x;
@@ -445,7 +447,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_fused_tc(float2 *a, const flo
                 const float2 *S;
                 uint32_t unit = 0;
                 if constexpr (PAIR) {
-                    const uint32_t k = 4u * (uint32_t)(it >> 1) + 2u * (uint32_t)(c0 / C::CHUNK) + (uint32_t)slice;
+                    const uint32_t k = (uint32_t)C::UNITS_PER_PAIR * (uint32_t)(it >> 1) +
+                                       2u * (uint32_t)(c0 / C::CHUNK) + (uint32_t)slice;
                     unit = k % NB;
                     if (!(it & 1) && !warp_wait_or_abort(raw_full + unit, (k / NB) & 1u, abort_flag, err_flag)) {
                         ok = false;
@@ -597,8 +600,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_fused_tc(float2 *a, const flo
                 bool ok = true;
                 for (uint32_t lp = 0; ok && tile_of(2 * (int)lp) < ntiles; ++lp) {
                     const uint64_t base = tile_base(g, tile_of(2 * (int)lp));
-                    for (uint32_t u = 0; u < 4; ++u) {
-                        const uint32_t k = 4 * lp + u, unit = k % NB;
+                    for (uint32_t u = 0; u < (uint32_t)C::UNITS_PER_PAIR; ++u) {
+                        const uint32_t k = (uint32_t)C::UNITS_PER_PAIR * lp + u, unit = k % NB;
                         if (k >= (uint32_t)NB &&
                             !wait_or_abort(raw_empty + unit, (k / NB - 1) & 1u, abort_flag, err_flag)) {
                             ok = false;

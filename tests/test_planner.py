@@ -311,3 +311,17 @@ def test_grouped_exponentials_random_runs(qi, orc, seed):
     assert any(op["kind"] == 10 and op["xmask"] == 0 and len(op["group"]) == 4 for op in ops)
     got = replay(ops, n, init)
     assert np.max(np.abs(got - want)) < 1e-12
+
+
+def test_window_partition_pass_counts(qi):
+    """The fuser's window candidates grow light-cone diamonds on brickwork circuits: the
+    30-qubit, 40-layer benchmark circuit (2260 gates) needs 80 dense blocks and 8 phase
+    polynomials (89 kernels with the renormalisation), where the first gate's light-cone
+    block alone needed 141 dense blocks; a bare QFT keeps its 11 dense blocks."""
+    n = 30
+    plan = qi.Plan(n, qi.F32, workloads.random_circuit(n, 40, seed=0), fusion=qi.FUSION_GREEDY, max_block_qubits=6)
+    kinds = [op["kind"] for op in plan.ops()]
+    assert kinds.count(4) == 80 and kinds.count(9) == 8 and len(kinds) == 89
+    qft = qi.Plan(n, qi.F32, workloads.qft(workloads.GateList(), list(range(n))).array(), fusion=qi.FUSION_GREEDY,
+                  max_block_qubits=6)
+    assert [op["kind"] for op in qft.ops()].count(4) <= 11

@@ -376,7 +376,8 @@ typedef struct qi_plan_op_info {
                                kind 10: number of exponentials in the run) */
     int32_t  targets[6];    /* sorted ascending for kinds 3, 4, 7 */
     int32_t  tensor_cores;  /* kind 4: 1 if the block runs on the tcgen05 tensor-core kernel */
-    int32_t  reserved;
+    int32_t  phase_poly;    /* kind 4: 1 if a phase polynomial (qi_plan_op_phase_poly) follows the block
+                               in the same pass */
     uint64_t control_mask;
     uint64_t xmask, zmask;  /* kinds 5 and 6; kind 9: zmask = the qubits the run touches;
                                kind 10: xmask = X, zmask = OR of the parity basis masks */
@@ -386,9 +387,10 @@ typedef struct qi_plan_op_info {
 } qi_plan_op_info;
 qi_status qi_plan_num_ops(const qi_plan *p, int64_t *out);
 qi_status qi_plan_op_get(const qi_plan *p, int64_t i, qi_plan_op_info *info, double *matrix_out, int64_t capacity);
-/* Kind 9 ops: the phase polynomial f(x) = c0 + sum_q a[q] x_q + sum_{q<r} b[q*n+r] x_q x_r
- * applied as exp(2 pi i f / 2^64) (coefficients in units of 2^-64 turns; a: n entries,
- * b: n*n entries, zero for q >= r).  Introspection aid; no reference counterpart. */
+/* Kind 9 ops, and kind 4 ops with phase_poly = 1 (applied after the block): the phase
+ * polynomial f(x) = c0 + sum_q a[q] x_q + sum_{q<r} b[q*n+r] x_q x_r applied as
+ * exp(2 pi i f / 2^64) (coefficients in units of 2^-64 turns; a: n entries, b: n*n entries,
+ * zero for q >= r).  Introspection aid; no reference counterpart. */
 qi_status qi_plan_op_phase_poly(const qi_plan *p, int64_t i, uint64_t *c0, uint64_t *a, uint64_t *b);
 /* Kind 10 ops: *n_tables tables (<= 4); table t is indexed by the parities
  * beta_j = popcount(i & basis[8 t + j]) & 1, j < rank[t] (index bit j = beta_j),

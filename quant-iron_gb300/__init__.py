@@ -217,13 +217,14 @@ class Plan:
                   "tensor_cores": info.tensor_cores,
                   "control_mask": info.control_mask, "xmask": info.xmask, "zmask": info.zmask,
                   "matrix": mat}
-            if info.kind == 9:   # phase polynomial: coefficients in units of 2^-64 turns
+            if info.kind == 9 or (info.kind == 4 and info.phase_poly):   # 2^-64 turns; kind 4: after the block
                 nq = self.num_qubits
                 c0 = ctypes.c_uint64()
                 a = np.zeros(nq, dtype=np.uint64)
                 b = np.zeros(nq * nq, dtype=np.uint64)
                 check(lib.qi_plan_op_phase_poly(self.h, i, ctypes.byref(c0), a.ctypes.data, b.ctypes.data))
-                op["targets"] = [q for q in range(nq) if (info.zmask >> q) & 1]
+                if info.kind == 9:
+                    op["targets"] = [q for q in range(nq) if (info.zmask >> q) & 1]
                 op["poly"] = (np.uint64(c0.value), a, b.reshape(nq, nq))
             if info.kind == 10:   # grouped Pauli exponentials: parity bases and their tables
                 nt = ctypes.c_int32()

@@ -82,7 +82,7 @@ class PlanStats(ctypes.Structure):
 
 class PlanOpInfo(ctypes.Structure):
     _fields_ = [("kind", ctypes.c_int32), ("k", ctypes.c_int32), ("targets", ctypes.c_int32 * 6),
-                ("tensor_cores", ctypes.c_int32), ("reserved", ctypes.c_int32),
+                ("tensor_cores", ctypes.c_int32), ("phase_poly", ctypes.c_int32),
                 ("control_mask", ctypes.c_uint64), ("xmask", ctypes.c_uint64), ("zmask", ctypes.c_uint64),
                 ("n_matrix", ctypes.c_int64)]
 

@@ -41,6 +41,18 @@ template <> struct Cx<double> {
     }
 };
 
+// exp(2 pi i f / 2^32) for a phase in fixed-point turns: T1[f >> 22] (T1 = exp(2 pi i j / 1024))
+// times exp(i x), x = the remaining 22 bits as an angle (< 2 pi / 1024), from the Taylor
+// polynomials of sin and cos to x^5 and x^4 (remainder < 1e-16).
+__device__ __forceinline__ float2 turn_phase(uint32_t f, const float2 *T1) {
+    const float2 t = T1[f >> 22];
+    const float x = (float)(f & 0x3FFFFFu) * 1.46291807926715968e-9f;   // 2 pi / 2^32
+    const float x2 = x * x;
+    const float s = x * (1.0f - x2 * (1.0f / 6.0f) * (1.0f - x2 * 0.05f));
+    const float c = 1.0f - x2 * 0.5f * (1.0f - x2 * (1.0f / 12.0f));
+    return make_float2(t.x * c - t.y * s, t.x * s + t.y * c);
+}
+
 // Streaming loads for data read exactly once (evict-first in L1/L2).
 __device__ static inline float4 ldg_stream(const float4 *p) { return __ldcs(p); }
 __device__ static inline double2 ldg_stream(const double2 *p) { return __ldcs(p); }

@@ -215,11 +215,13 @@ Status launch_fused_simt(qi_state *s, int k, const int32_t *targets, const void 
     }
 }
 
-Status launch_fused(qi_state *s, int k, const int32_t *targets, const void *d_mat, const void *d_tc, int use_tc) {
+Status launch_fused(qi_state *s, int k, const int32_t *targets, const void *d_mat, const void *d_tc, int use_tc,
+                    const void *poly) {
     const int n = s->n;
     if (k < 1 || k > 6 || k > n) return err(QI_ERR_INVALID_INPUT_VALUE, k, n, "fused block width");
     if (s->prec == QI_F64 && k > 5) return err(QI_ERR_UNSUPPORTED, k, -1, "FP64 fused blocks are limited to k <= 5");
-    if (use_tc && d_tc && s->prec == QI_F32 && k >= 5 && n >= k + 7) return launch_fused_tc(s, k, targets, d_tc);
+    if (use_tc && d_tc && s->prec == QI_F32 && k >= 5 && n >= k + 7) return launch_fused_tc(s, k, targets, d_tc, poly);
+    if (poly) return err(QI_ERR_UNKNOWN, k, n, "a phase polynomial rides only on a tensor-core block");
     return launch_fused_simt(s, k, targets, d_mat);
 }
 

@@ -250,6 +250,13 @@ __device__ __forceinline__ bool warp_wait_or_abort(uint64_t *bar, uint32_t parit
     return __all_sync(0xffffffffu, ok);
 }
 
+// Phase table of a tensor-core block that carries a phase polynomial (32-bit words, 2^-32 turns):
+// [0, 64) the terms among each row's bits; [kPhaseLane, +128 x 8) per column index m: the terms
+// among its column bits, then its cross terms with each row bit j; [kPhaseTile, +16 per tile):
+// c0 + the terms among the tile's bits, its cross terms with column bit b (1 + b) and with row
+// bit j (8 + j).
+constexpr int kPhaseLane = 64, kPhaseTile = 64 + 128 * 8;
+
 // ------------------------------------------------------------------ kernel
 template <int K, bool PAIR = false>
 struct TcCfg {
@@ -276,7 +283,8 @@ struct TcCfg {
     static constexpr size_t OFF_BAR = OFF_GROW + 64 * sizeof(uint64_t);
     static constexpr int NBARS = 2 * NBUF + 9;
     static constexpr size_t OFF_MISC = OFF_BAR + NBARS * sizeof(uint64_t);
-    static constexpr size_t SMEM = OFF_MISC + 16;
+    static constexpr size_t OFF_FR = OFF_MISC + 16;    // phase polynomial: terms among each row's bits
+    static constexpr size_t SMEM = OFF_FR + 64 * sizeof(uint32_t);
 };
 
 // Tile-local position of column m: its bits deposited, in order, on the bits
@@ -344,8 +352,11 @@ __device__ __forceinline__ void st_cs_v8(float2 *p, float a0, float a1, float a2
 // ROT: qubits 0-3 are all targets, so the tile's columns are 128 bytes or more apart and the
 // 8 lanes of a quarter warp would read the same banks for one row pair; each lane then reads the
 // chunk's row pairs starting at its own (lane mod 8), undone in registers.
-template <int K, bool PAIR, bool ROT>
-__global__ void __launch_bounds__(kTcThreads, 1) k_fused_tc(float2 *a, const float *blocks, TileGeom g, int *err_flag) {
+// PHASE: a diagonal phase polynomial exp(2 pi i f(x)) that follows the block in the plan is
+// applied by the epilogue before the store (its phase table at `poly`, tc_phase_table).
+template <int K, bool PAIR, bool ROT, bool PHASE>
+__global__ void __launch_bounds__(kTcThreads, 1) k_fused_tc(float2 *a, const float *blocks, TileGeom g, int *err_flag,
+                                                            const uint32_t *__restrict__ poly) {
     using C = TcCfg<K, PAIR>;
     constexpr int R = C::R, NB = C::NBUF;
     static_assert(!PAIR || (K == 6 && C::UNIT_ROWS == C::CHUNK), "pair mode: K = 6, one ring unit per chunk");
@@ -533,11 +544,35 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_fused_tc(float2 *a, const flo
     } else if (warp < kConvWarps + kEpiWarps) {
         // ------------------------------------------------ epilogue
         const int quarter = warp & 3;
-        const uint64_t cx = tile_colx(g, (uint32_t)(quarter * 32 + lane));
+        const uint32_t m = (uint32_t)(quarter * 32 + lane);
+        const uint64_t cx = tile_colx(g, m);
         const uint32_t lane_base = (uint32_t)(quarter * 32) << 16;
+        // Phase polynomial f(i) = c0 + sum_q a_q i_q + sum_{q<r} b_qr i_q i_r (2^-32 turns, wrapping)
+        // over i = tile bits | column bits | row bits, from the host table (tc_phase_table): the
+        // terms among a row's bits (FR), among this lane's column bits (p_lane) and the column-row
+        // cross terms (wz[j] per row bit j) once; the tile terms once per tile.
+        uint32_t p_lane = 0, wz[K], *FR = reinterpret_cast<uint32_t *>(smem_raw + C::OFF_FR);
+        if constexpr (PHASE) {
+#pragma unroll
+            for (int j = 0; j < K; ++j) wz[j] = __ldg(poly + kPhaseLane + m * 8 + 1 + j);
+            p_lane = __ldg(poly + kPhaseLane + m * 8);
+            const int e = (warp - kConvWarps) * 32 + lane;
+            if (e < R) FR[e] = __ldg(poly + e);
+            asm volatile("bar.sync 1, %0;\n" ::"r"(kEpiWarps * 32) : "memory");   // the epilogue warps only
+        }
         for (int it = 0; tile_of(it) < ntiles; ++it) {
             const uint32_t t = tile_of(it);
             const int d = it & 1;
+            uint32_t pbase = 0, z[K];
+            if constexpr (PHASE) {   // c0 + the tile's own terms, its cross terms with columns / rows
+                const uint32_t *tt = poly + kPhaseTile + (size_t)t * 16;
+                pbase = p_lane + __ldg(tt);
+#pragma unroll
+                for (int b = 0; b < 7; ++b)
+                    if ((m >> b) & 1u) pbase += __ldg(tt + 1 + b);
+#pragma unroll
+                for (int j = 0; j < K; ++j) z[j] = wz[j] + __ldg(tt + 8 + j);
+            }
             if (!warp_wait_or_abort(d_full + d, (uint32_t)(it >> 1) & 1u, abort_flag, err_flag)) break;
             tc_fence_after();
             float2 *out = a + (tile_base(g, t) | cx);   // column base; rows add disjoint bits
@@ -552,6 +587,24 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_fused_tc(float2 *a, const flo
                     tc_fence_before();
                     __syncwarp();
                     if (lane == 0) mbar_arrive(d_empty + d);
+                }
+                if constexpr (PHASE) {
+#pragma unroll
+                    for (int i = 0; i < 16; ++i) {
+                        const int r = 16 * c + i;   // compile-time after unrolling
+                        uint32_t f = pbase + FR[r];
+#pragma unroll
+                        for (int j = 0; j < K; ++j)
+                            if ((r >> j) & 1) f += z[j];
+                        // the angle as a signed fraction of a turn, in [-pi, pi): the SFU's sin / cos
+                        // (absolute error about 2^-21, the order of the FP32 state's own rounding)
+                        float sn, cs;
+                        __sincosf((float)(int32_t)f * 1.46291807926715968e-9f, &sn, &cs);   // 2 pi / 2^32
+                        const float2 ph = make_float2(cs, sn);
+                        const float xr = __uint_as_float(vr[i]), xi = __uint_as_float(vi[i]);
+                        vr[i] = __float_as_uint(ph.x * xr - ph.y * xi);
+                        vi[i] = __float_as_uint(ph.x * xi + ph.y * xr);
+                    }
                 }
                 if (quad_rows) {
 #pragma unroll
@@ -718,14 +771,98 @@ void tc_blocks(int k, const double *U, std::vector<float> &out) {
     }
 }
 
-template <int K, bool PAIR, bool ROT>
-static Status launch_tc_t(qi_state *s, const TileGeom &g, const void *d_tc) {
+// Host: the phase table of a block on `targets` that carries the phase polynomial pp (layout
+// at kPhaseLane / kPhaseTile).  Coefficients are rounded to 2^-32 turns one by one and summed
+// with wrapping, as the standalone phase-polynomial kernel does.  Tiles are visited in Gray-code
+// order, so each tile's terms follow from the previous tile's by one qubit.  False (nothing
+// appended) beyond 2^20 tiles (16 words each).
+bool tc_phase_table(const PhasePoly &pp, int k, const int32_t *targets, std::vector<float> &out) {
+    const int n = pp.n;
+    const TileGeom g = make_tile_geom(n, k, targets, 7);
+    if (g.nfree > 20 || k > 6) return false;
+    auto r32 = [](uint64_t v) { return (uint32_t)((v + 0x80000000ull) >> 32); };
+    auto A = [&](int q) { return r32(pp.a[(size_t)q]); };
+    auto B = [&](int q, int r) -> uint32_t {
+        if (q == r) return 0u;
+        if (q > r) std::swap(q, r);
+        return r32(pp.b[(size_t)q * n + r]);
+    };
+    int tq[6] = {0, 0, 0, 0, 0, 0}, colq[7] = {0, 0, 0, 0, 0, 0, 0};
+    for (int j = 0; j < k; ++j) tq[j] = j < g.nlow_t ? g.low_t[j] : g.high_t[j - g.nlow_t];
+    for (int q = 0, b = 0; q < g.L && b < 7; ++q) {   // the 7 lowest non-target qubits, in order
+        bool tgt = false;
+        for (int u = 0; u < g.nlow_t; ++u) tgt |= g.low_t[u] == q;
+        if (!tgt) colq[b++] = q;
+    }
+    auto host_tile_base = [&](uint64_t t) {
+        uint64_t base = 0;
+        for (int j = 0; j < g.nruns; ++j) base |= ((t >> g.run_src[j]) & g.run_mask[j]) << g.run_dst[j];
+        return base;
+    };
+    int fq[64];
+    for (int j = 0; j < g.nfree; ++j) fq[j] = __builtin_ctzll(host_tile_base(1ull << j));
+    const size_t ntiles = (size_t)g.ntiles;
+    std::vector<uint32_t> w((size_t)kPhaseTile + 16 * ntiles, 0);
+    for (int r = 0; r < (1 << k); ++r) {   // terms among a row's bits
+        uint32_t v = 0;
+        for (int j = 0; j < k; ++j) {
+            if (!((r >> j) & 1)) continue;
+            v += A(tq[j]);
+            for (int j2 = 0; j2 < j; ++j2)
+                if ((r >> j2) & 1) v += B(tq[j], tq[j2]);
+        }
+        w[(size_t)r] = v;
+    }
+    for (int m = 0; m < 128; ++m) {   // per column index: its own terms, cross terms with each row bit
+        uint32_t pl = 0;
+        for (int b = 0; b < 7; ++b) {
+            if (!((m >> b) & 1)) continue;
+            pl += A(colq[b]);
+            for (int b2 = 0; b2 < b; ++b2)
+                if ((m >> b2) & 1) pl += B(colq[b], colq[b2]);
+        }
+        w[(size_t)kPhaseLane + (size_t)m * 8] = pl;
+        for (int j = 0; j < k; ++j) {
+            uint32_t v = 0;
+            for (int b = 0; b < 7; ++b)
+                if ((m >> b) & 1) v += B(colq[b], tq[j]);
+            w[(size_t)kPhaseLane + (size_t)m * 8 + 1 + (size_t)j] = v;
+        }
+    }
+    uint32_t pt = r32(pp.c0), U[7] = {0, 0, 0, 0, 0, 0, 0}, V[6] = {0, 0, 0, 0, 0, 0};
+    uint64_t cur = 0;   // tile bits of the current tile
+    auto store = [&](uint64_t t) {
+        uint32_t *o = w.data() + kPhaseTile + (size_t)t * 16;
+        o[0] = pt;
+        for (int b = 0; b < 7; ++b) o[1 + b] = U[b];
+        for (int j = 0; j < k; ++j) o[8 + j] = V[j];
+    };
+    store(0);
+    for (uint64_t i = 1; i < (uint64_t)ntiles; ++i) {   // Gray code: tile i ^ (i >> 1) flips bit ctz(i)
+        const int j = __builtin_ctzll(i), q = fq[j];
+        const bool on = !((cur >> j) & 1ull);
+        uint32_t delta = A(q);
+        for (uint64_t rest = cur & ~(1ull << j); rest; rest &= rest - 1) delta += B(q, fq[__builtin_ctzll(rest)]);
+        pt += on ? delta : (uint32_t)(0u - delta);
+        for (int b = 0; b < 7; ++b) U[b] += on ? B(q, colq[b]) : (uint32_t)(0u - B(q, colq[b]));
+        for (int jj = 0; jj < k; ++jj) V[jj] += on ? B(q, tq[jj]) : (uint32_t)(0u - B(q, tq[jj]));
+        cur ^= 1ull << j;
+        store(cur);
+    }
+    const size_t base = out.size();
+    out.resize(base + w.size(), 0.0f);
+    std::memcpy(out.data() + base, w.data(), w.size() * 4);
+    return true;
+}
+
+template <int K, bool PAIR, bool ROT, bool PHASE>
+static Status launch_tc_t(qi_state *s, const TileGeom &g, const void *d_tc, const void *poly) {
     using C = TcCfg<K, PAIR>;
     static_assert(C::SMEM <= 232448, "shared memory per CTA");
     static bool attr_set = false;
     static int num_sms = 0;
     if (!attr_set) {
-        QI_CUDA(cudaFuncSetAttribute(k_fused_tc<K, PAIR, ROT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::SMEM));
+        QI_CUDA(cudaFuncSetAttribute(k_fused_tc<K, PAIR, ROT, PHASE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::SMEM));
         int dev = 0;
         QI_CUDA(cudaGetDevice(&dev));
         QI_CUDA(cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, dev));
@@ -733,13 +870,13 @@ static Status launch_tc_t(qi_state *s, const TileGeom &g, const void *d_tc) {
     }
     uint64_t grid = PAIR ? g.ntiles / 2 : g.ntiles;   // one persistent CTA per SM
     if (grid > (uint64_t)num_sms) grid = (uint64_t)num_sms;
-    k_fused_tc<K, PAIR, ROT><<<(unsigned)grid, kTcThreads, C::SMEM, s->stream>>>((float2 *)s->amps, (const float *)d_tc,
-                                                                            g, s->d_flag);
+    k_fused_tc<K, PAIR, ROT, PHASE><<<(unsigned)grid, kTcThreads, C::SMEM, s->stream>>>(
+        (float2 *)s->amps, (const float *)d_tc, g, s->d_flag, (const uint32_t *)poly);
     count_launch();
     return check_launch("k_fused_tc");
 }
 
-Status launch_fused_tc(qi_state *s, int k, const int32_t *targets, const void *d_tc) {
+Status launch_fused_tc(qi_state *s, int k, const int32_t *targets, const void *d_tc, const void *poly) {
     const int n = s->n;
     if (s->prec != QI_F32 || (k != 5 && k != 6) || n < k + 7)
         return err(QI_ERR_UNSUPPORTED, k, n, "tensor-core blocks need FP32, k in {5, 6}, n >= k + 7");
@@ -754,9 +891,13 @@ Status launch_fused_tc(qi_state *s, int k, const int32_t *targets, const void *d
     // qubits 0-3 all targets: lane-rotated row reads (k_fused_tc's ROT)
     bool rot = true;
     for (int q = 0; q < 4; ++q) rot = rot && std::find(targets, targets + k, q) != targets + k;
-    if (k == 5) return rot ? launch_tc_t<5, false, true>(s, g, d_tc) : launch_tc_t<5, false, false>(s, g, d_tc);
-    if (pair) return launch_tc_t<6, true, false>(s, g, d_tc);
-    return rot ? launch_tc_t<6, false, true>(s, g, d_tc) : launch_tc_t<6, false, false>(s, g, d_tc);
+    if (poly && ((uintptr_t)poly & 15) != 0) return err(QI_ERR_UNKNOWN, -1, -1, "phase block must be 16-byte aligned");
+#define QI_TC(KK, PA, RO)                                                                    \
+    (poly ? launch_tc_t<KK, PA, RO, true>(s, g, d_tc, poly) : launch_tc_t<KK, PA, RO, false>(s, g, d_tc, nullptr))
+    if (k == 5) return rot ? QI_TC(5, false, true) : QI_TC(5, false, false);
+    if (pair) return QI_TC(6, true, false);
+    return rot ? QI_TC(6, false, true) : QI_TC(6, false, false);
+#undef QI_TC
 }
 
 }  // namespace qi

@@ -558,7 +558,8 @@ Status launch_op(qi_state *s, const Op &op, const void *d_mats, const void *d_tc
         const size_t esz = f32 ? sizeof(float2) : sizeof(double2);
         const char *mp = (const char *)d_mats + (size_t)op.mat_offset * esz;
         const void *tp = (d_tc && op.tc_offset >= 0) ? (const void *)((const float *)d_tc + op.tc_offset) : nullptr;
-        return launch_fused(s, op.k, op.targets, mp, tp, op.mode);
+        const void *pp = (d_tc && op.poly_tc >= 0) ? (const void *)((const float *)d_tc + op.poly_tc) : nullptr;
+        return launch_fused(s, op.k, op.targets, mp, tp, op.mode, pp);
     }
     case OP_NORMALISE:
         return state_normalise_device_async(s);

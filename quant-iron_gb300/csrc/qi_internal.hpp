@@ -112,6 +112,9 @@ struct Op {
     uint64_t xmask = 0, zmask = 0; // Pauli ops
     double alpha_re = 0, alpha_im = 0;   // Pauli exp: cosh/sinh coefficients are derived from this
     double cre = 0, cim = 0, sre = 0, sim = 0;
+    // OP_FUSED on the tensor cores: a phase polynomial applied after the block in the same pass
+    // (its device block at tc offset poly_tc, its host copy plan->polys[poly_idx]), or -1
+    int64_t poly_tc = -1, poly_idx = -1;
     // OP_PAULI_GROUP: table c is indexed by the parities popc(i & basis[c * kGroupRank + j]) & 1,
     // j < rank[c] (pair groups: i = the partner with the highest bit of xmask clear)
     int32_t nchunk = 0;
@@ -156,10 +159,12 @@ Status launch_pauli_group(qi_state *s, const Op &op, const void *d_mats);
 // ------------------------------------------------------------------ fused --
 // Apply a dense 2^k x 2^k complex matrix (device pointer, row-major, element
 // type matches the state's precision) on sorted targets.
-Status launch_fused(qi_state *s, int k, const int32_t *targets, const void *d_mat, const void *d_tc, int use_tc);
+Status launch_fused(qi_state *s, int k, const int32_t *targets, const void *d_mat, const void *d_tc, int use_tc,
+                    const void *poly = nullptr);
 // 3xTF32 tcgen05 kernel (FP32 states, k = 5 or 6, n >= k + 7); d_tc holds the
 // six operand blocks prepared by tc_blocks().
-Status launch_fused_tc(qi_state *s, int k, const int32_t *targets, const void *d_tc);
+// poly: device block of a phase polynomial applied after the block in the same pass (or null)
+Status launch_fused_tc(qi_state *s, int k, const int32_t *targets, const void *d_tc, const void *poly = nullptr);
 // Host: the six K-major operand blocks {-Im U, Re U, Im U} x {tf32 hi, lo}
 // (each 2^k x 2^k floats in the no-swizzle core-matrix layout) of a fused
 // matrix U (row-major complex, FP64).  Appends 6 * 4^k floats to `out`.
@@ -189,7 +194,13 @@ bool phase_poly_add_table(PhasePoly &pp, int k, const int32_t *qubits, const std
 // Iteration bits h of the phase-polynomial kernel for n qubits (FP32 states).
 int phase_poly_iter_bits(int n);
 // Device block of pp (32-bit words) appended to `out`, padded to 16 bytes.
+// Device block of a phase polynomial (32-bit words): a[q] at kPolyA, b[q][r] (symmetric,
+// 64 x 64) at kPolyB, the exp table T1 (1024 x float2) at kPolyT1, c0 + iteration tables at kPolyG0.
+constexpr int kPolyA = 0, kPolyB = 64, kPolyT1 = 64 + 64 * 64, kPolyG0 = kPolyT1 + 2 * 1024;
 void phase_poly_device_block(const PhasePoly &pp, std::vector<float> &out);
+// The phase table a tensor-core block on `targets` (sorted) uses to apply pp after the block in
+// its epilogue (qi_fused_tc.cu); false (nothing appended) when the state has too many tiles.
+bool tc_phase_table(const PhasePoly &pp, int k, const int32_t *targets, std::vector<float> &out);
 Status launch_phase_poly(qi_state *s, const void *d_block);
 
 }  // namespace qi

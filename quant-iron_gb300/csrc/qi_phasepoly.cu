@@ -28,14 +28,13 @@
 // T1 = exp(2 pi i j / 1024) (1024 entries, rounded from FP64 on the host) and
 // the Taylor polynomials of sin and cos to x^5 and x^4 (remainder < 1e-16).
 #include "qi_internal.hpp"
+#include "qi_device.cuh"
 
 #include <cmath>
 
 namespace qi {
 
 constexpr int kPolyThreads = 256, kPolyMaxH = 12, kPolyUnroll = 8;
-// device block layout (32-bit words)
-constexpr int kPolyA = 0, kPolyB = 64, kPolyT1 = 64 + 64 * 64, kPolyG0 = kPolyT1 + 2 * 1024;
 
 static uint64_t turns64(double angle_rad) {
     double t = angle_rad / (2.0 * M_PI);          // (-0.5, 0.5]
@@ -127,15 +126,6 @@ void phase_poly_device_block(const PhasePoly &pp, std::vector<float> &out) {
     const size_t padded = (words + 3) & ~(size_t)3;
     out.resize(base + padded, 0.0f);
     std::memcpy(out.data() + base, w.data(), words * 4);
-}
-
-__device__ __forceinline__ float2 turn_phase(uint32_t f, const float2 *T1) {
-    const float2 t = T1[f >> 22];
-    const float x = (float)(f & 0x3FFFFFu) * 1.46291807926715968e-9f;   // 2 pi / 2^32
-    const float x2 = x * x;
-    const float s = x * (1.0f - x2 * (1.0f / 6.0f) * (1.0f - x2 * 0.05f));
-    const float c = 1.0f - x2 * 0.5f * (1.0f - x2 * (1.0f / 12.0f));
-    return make_float2(t.x * c - t.y * s, t.x * s + t.y * c);
 }
 
 __global__ void __launch_bounds__(kPolyThreads) k_phase_poly(float4 *v, const uint32_t *blk, int m, int h) {

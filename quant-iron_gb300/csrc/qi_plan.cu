@@ -363,9 +363,17 @@ Status build_plan(qi_plan *p, std::vector<Elem> &elems) {
                     for (int j = 0; j < d.k; ++j) op.zmask |= 1ull << d.targets[j];
                 op.mat_offset = (int64_t)p->polys.size();
                 op.tc_offset = (int64_t)p->tc.size();
-                phase_poly_device_block(pending, p->tc);
                 p->polys.push_back(pending);
-                p->ops.push_back(op);
+                Op *prev = p->ops.empty() ? nullptr : &p->ops.back();
+                if (prev && prev->kind == OP_FUSED && prev->tc_offset >= 0 && prev->poly_tc < 0 &&
+                    tc_phase_table(pending, prev->k, prev->targets, p->tc)) {
+                    // right after a tensor-core block: its epilogue applies the phases (no extra pass)
+                    prev->poly_tc = op.tc_offset;
+                    prev->poly_idx = op.mat_offset;
+                } else {
+                    phase_poly_device_block(pending, p->tc);
+                    p->ops.push_back(op);
+                }
             } else if (pending_ops.size() == 1) {
                 p->ops.push_back(pending_ops[0]);
             }
@@ -659,9 +667,10 @@ qi_status qi_plan_op_phase_poly(const qi_plan *p, int64_t i, uint64_t *c0, uint6
     if (!p || !c0 || !a || !b) return publish(err(QI_ERR_NULL_ARGUMENT));
     if (i < 0 || i >= (int64_t)p->ops.size()) return publish(err(QI_ERR_INVALID_INPUT_VALUE, i));
     const Op &op = p->ops[(size_t)i];
-    if (op.kind != OP_PHASE_POLY || op.mat_offset < 0 || op.mat_offset >= (int64_t)p->polys.size())
-        return publish(err(QI_ERR_INVALID_INPUT_VALUE, i, op.kind, "not a phase-polynomial op"));
-    const PhasePoly &pp = p->polys[(size_t)op.mat_offset];
+    const int64_t idx = op.kind == OP_PHASE_POLY ? op.mat_offset : op.kind == OP_FUSED ? op.poly_idx : -1;
+    if (idx < 0 || idx >= (int64_t)p->polys.size())
+        return publish(err(QI_ERR_INVALID_INPUT_VALUE, i, op.kind, "no phase polynomial on this op"));
+    const PhasePoly &pp = p->polys[(size_t)idx];
     *c0 = pp.c0;
     std::copy(pp.a.begin(), pp.a.end(), a);
     std::copy(pp.b.begin(), pp.b.end(), b);
@@ -688,6 +697,7 @@ qi_status qi_plan_op_get(const qi_plan *p, int64_t i, qi_plan_op_info *info, dou
     info->k = op.k;
     for (int j = 0; j < 6; ++j) info->targets[j] = op.targets[j];
     info->tensor_cores = (op.kind == OP_FUSED && op.tc_offset >= 0) ? 1 : 0;
+    info->phase_poly = (op.kind == OP_FUSED && op.poly_idx >= 0) ? 1 : 0;
     info->control_mask = op.cmask;
     info->xmask = op.xmask;
     info->zmask = op.zmask;

@@ -30,15 +30,21 @@ def test_phase_poly_plan_vs_oracle(qi, orc, n, kmax):
     assert 1 - abs(np.vdot(want, got)) ** 2 / np.vdot(got, got).real < 1e-9
 
 
+@pytest.mark.parametrize("tensor_cores", [2, 1], ids=["standalone", "in_tc_epilogue"])
 @pytest.mark.parametrize("n", [23, 27])
-def test_phase_poly_many_iterations_vs_per_gate(qi, n):
+def test_phase_poly_many_iterations_vs_per_gate(qi, n, tensor_cores):
     """n = 23 and 27: 2^5 and 2^9 iterations per thread (the iteration-bit tables
     and per-thread cross terms are exercised); compared with the per-gate FP32
-    execution of the same QFT."""
+    execution of the same QFT.  With CUDA-core blocks the polynomials run as their own
+    pass (k_phase_poly); after a tensor-core block they ride on its epilogue."""
     gates = workloads.qft(workloads.GateList(), list(range(n))).array()
     init_gates = workloads.random_circuit(n, 1, seed=2, with_qft=False)
-    fused = qi.Plan(n, qi.F32, gates, fusion=qi.FUSION_GREEDY, max_block_qubits=6)
-    assert sum(op["kind"] == 9 for op in fused.ops()) >= 2
+    fused = qi.Plan(n, qi.F32, gates, fusion=qi.FUSION_GREEDY, max_block_qubits=6, use_tensor_cores=tensor_cores)
+    ops = fused.ops()
+    if tensor_cores == 2:
+        assert sum(op["kind"] == 9 for op in ops) >= 2
+    else:
+        assert sum(op["kind"] == 4 and "poly" in op for op in ops) >= 2
     with qi.DeviceState(n, qi.F32) as a, qi.DeviceState(n, qi.F32) as b:
         for s in (a, b):
             s.set_plus()

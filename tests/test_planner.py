@@ -61,6 +61,8 @@ def replay(ops, n, init):
             s = _apply_local(s, n, op["targets"][:2], op["matrix"], op["control_mask"])
         elif kind == 4:
             s = _apply_local(s, n, op["targets"], op["matrix"], 0)
+            if "poly" in op:   # a phase polynomial applied after the block in the same pass
+                s = s * poly_phases(op["poly"], n)
         elif kind == 7:
             s = _apply_local(s, n, op["targets"], np.diag(op["matrix"]).reshape(-1), 0)
         elif kind == 9:
@@ -316,12 +318,15 @@ def test_grouped_exponentials_random_runs(qi, orc, seed):
 def test_window_partition_pass_counts(qi):
     """The fuser's window candidates grow light-cone diamonds on brickwork circuits: the
     30-qubit, 40-layer benchmark circuit (2260 gates) needs 80 dense blocks and 8 phase
-    polynomials (89 kernels with the renormalisation), where the first gate's light-cone
-    block alone needed 141 dense blocks; a bare QFT keeps its 11 dense blocks."""
+    polynomials, where the first gate's light-cone block alone needed 141 dense blocks; a
+    bare QFT keeps its 11 dense blocks."""
     n = 30
     plan = qi.Plan(n, qi.F32, workloads.random_circuit(n, 40, seed=0), fusion=qi.FUSION_GREEDY, max_block_qubits=6)
-    kinds = [op["kind"] for op in plan.ops()]
-    assert kinds.count(4) == 80 and kinds.count(9) == 8 and len(kinds) == 89
+    ops = plan.ops()
+    kinds = [op["kind"] for op in ops]
+    # each phase polynomial right after a tensor-core block rides on that block's pass
+    assert kinds.count(4) == 80 and kinds.count(9) + sum("poly" in op for op in ops) == 8
+    assert len(kinds) == 81 + kinds.count(9)
     qft = qi.Plan(n, qi.F32, workloads.qft(workloads.GateList(), list(range(n))).array(), fusion=qi.FUSION_GREEDY,
                   max_block_qubits=6)
     assert [op["kind"] for op in qft.ops()].count(4) <= 11

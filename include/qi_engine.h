@@ -111,6 +111,14 @@ qi_status qi_state_synchronize(qi_state *s);
 qi_status qi_state_upload(qi_state *s, const double *amps, uint64_t num_amps);
 /* Copy the device state back as interleaved f64 pairs (operator.rs:137-147). */
 qi_status qi_state_download(qi_state *s, double *amps, uint64_t num_amps);
+/* Asynchronous forms for page-locked host buffers: the transfer runs on the copy
+ * engine (no SM time) through a device staging buffer of the FP64 size, converted
+ * by one device pass, in the handle's stream order; the call returns at once and
+ * the host buffer must stay untouched (upload) or is complete (download) only after
+ * qi_state_synchronize.  Lets a caller keep two states in flight, one transferring
+ * while the other computes.  A pageable host buffer returns InvalidInputValue. */
+qi_status qi_state_upload_async(qi_state *s, const double *amps, uint64_t num_amps);
+qi_status qi_state_download_async(qi_state *s, double *amps, uint64_t num_amps);
 
 /* Device-side constructors: State::new_zero / new_basis_n / new_plus /
  * new_minus / new_ghz (state.rs:165-325), filled in place. */

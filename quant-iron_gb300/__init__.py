@@ -111,6 +111,16 @@ class DeviceState:
     def download_ptr(self, host_ptr, num_amps):
         check(lib.qi_state_download(self.h, ctypes.c_void_p(host_ptr), int(num_amps)))
 
+    def upload_async(self, host_ptr, num_amps):
+        """Upload from a page-locked host buffer on the copy engine, in this state's stream
+        order; the buffer must stay untouched until synchronize()."""
+        check(lib.qi_state_upload_async(self.h, ctypes.c_void_p(host_ptr), int(num_amps)))
+
+    def download_async(self, host_ptr, num_amps):
+        """Download into a page-locked host buffer on the copy engine; complete after
+        synchronize()."""
+        check(lib.qi_state_download_async(self.h, ctypes.c_void_p(host_ptr), int(num_amps)))
+
     def set_zero(self):
         check(lib.qi_state_set_zero(self.h))
 

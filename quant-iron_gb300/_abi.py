@@ -108,6 +108,8 @@ SIGNATURES = {
     "qi_state_synchronize": (_i32, [_vp]),
     "qi_state_upload": (_i32, [_vp, _vp, _u64]),
     "qi_state_download": (_i32, [_vp, _vp, _u64]),
+    "qi_state_upload_async": (_i32, [_vp, _vp, _u64]),
+    "qi_state_download_async": (_i32, [_vp, _vp, _u64]),
     "qi_state_set_zero": (_i32, [_vp]),
     "qi_state_set_basis": (_i32, [_vp, _u64]),
     "qi_state_set_plus": (_i32, [_vp]),

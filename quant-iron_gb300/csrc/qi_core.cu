@@ -522,6 +522,48 @@ qi_status qi_state_upload(qi_state *s, const double *amps, uint64_t num_amps) {
     return publish(check_launch("k_convert"));
 }
 
+qi_status qi_state_upload_async(qi_state *s, const double *amps, uint64_t num_amps) {
+    QI_GUARD(s);
+    if (!amps) return publish(err(QI_ERR_NULL_ARGUMENT));
+    if (num_amps != s->dim()) return publish(err(QI_ERR_INVALID_NUMBER_OF_QUBITS, s->n));
+    if (!mapped_host_ptr(amps)) return publish(err(QI_ERR_INVALID_INPUT_VALUE, -1, -1, "host buffer not page-locked"));
+    if (s->prec == QI_F64) {
+        cudaError_t e = cudaMemcpyAsync(s->amps, amps, s->bytes(), cudaMemcpyHostToDevice, s->stream);
+        if (e != cudaSuccess) return publish(cuda_status(e, "upload_async"));
+        return publish(ok_status());
+    }
+    Status st = ensure_staging(s, num_amps * 16);
+    if (!st.ok()) return publish(st);
+    cudaError_t e = cudaMemcpyAsync(s->d_staging, amps, num_amps * 16, cudaMemcpyHostToDevice, s->stream);
+    if (e != cudaSuccess) return publish(cuda_status(e, "upload_async"));
+    k_convert<float, double><<<grid_for(num_amps), 256, 0, s->stream>>>((float2 *)s->amps,
+                                                                        (const double2 *)s->d_staging, num_amps);
+    count_launch();
+    return publish(check_launch("k_convert"));
+}
+
+qi_status qi_state_download_async(qi_state *s, double *amps, uint64_t num_amps) {
+    QI_GUARD(s);
+    if (!amps) return publish(err(QI_ERR_NULL_ARGUMENT));
+    if (num_amps != s->dim()) return publish(err(QI_ERR_INVALID_NUMBER_OF_QUBITS, s->n));
+    if (!mapped_host_ptr(amps)) return publish(err(QI_ERR_INVALID_INPUT_VALUE, -1, -1, "host buffer not page-locked"));
+    if (s->prec == QI_F64) {
+        cudaError_t e = cudaMemcpyAsync(amps, s->amps, s->bytes(), cudaMemcpyDeviceToHost, s->stream);
+        if (e != cudaSuccess) return publish(cuda_status(e, "download_async"));
+        return publish(ok_status());
+    }
+    Status st = ensure_staging(s, num_amps * 16);
+    if (!st.ok()) return publish(st);
+    k_convert<double, float><<<grid_for(num_amps), 256, 0, s->stream>>>((double2 *)s->d_staging,
+                                                                        (const float2 *)s->amps, num_amps);
+    count_launch();
+    st = check_launch("k_convert");
+    if (!st.ok()) return publish(st);
+    cudaError_t e = cudaMemcpyAsync(amps, s->d_staging, num_amps * 16, cudaMemcpyDeviceToHost, s->stream);
+    if (e != cudaSuccess) return publish(cuda_status(e, "download_async"));
+    return publish(ok_status());
+}
+
 qi_status qi_state_download(qi_state *s, double *amps, uint64_t num_amps) {
     QI_GUARD(s);
     if (!amps) return publish(err(QI_ERR_NULL_ARGUMENT));

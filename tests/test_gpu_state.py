@@ -164,3 +164,44 @@ def test_mirror_chain_stays_on_device(qi):
     assert st._host is not None and abs(np.vdot(v, v) - 1.0) < 1e-12
     st.state_vector = ka.zero(12)
     assert st._dev is None and st.h(0).x(0).probability(1) == pytest.approx(0.5)
+
+
+@pytest.mark.parametrize("prec", [0, 1], ids=["f64", "f32"])
+def test_async_transfers_roundtrip_and_overlap(qi, prec):
+    """upload_async / download_async (copy engine, page-locked buffers) match the synchronous
+    path bit for bit; two states keep their own stream order while both are in flight; a
+    pageable buffer is refused."""
+    torch = pytest.importorskip("torch")
+    n = 20
+    v = rand_state(n, 7)
+    w = rand_state(n, 8)
+    host_v = torch.empty(2 << n, dtype=torch.float64, pin_memory=True)
+    host_w = torch.empty(2 << n, dtype=torch.float64, pin_memory=True)
+    host_v.numpy()[:] = v.view(np.float64)
+    host_w.numpy()[:] = w.view(np.float64)
+    out_a = torch.zeros(2 << n, dtype=torch.float64, pin_memory=True)
+    out_b = torch.zeros(2 << n, dtype=torch.float64, pin_memory=True)
+    with qi.DeviceState(n, prec) as a, qi.DeviceState(n, prec) as b:
+        a.upload_async(host_v.data_ptr(), 1 << n)
+        b.upload_async(host_w.data_ptr(), 1 << n)
+        a.apply_gate(qi_gate_row(qi, "H", [3]))
+        b.apply_gate(qi_gate_row(qi, "X", [19]))
+        a.download_async(out_a.data_ptr(), 1 << n)
+        b.download_async(out_b.data_ptr(), 1 << n)
+        a.synchronize()
+        b.synchronize()
+        sync_a = a.download()
+        sync_b = b.download()
+        with pytest.raises(qi.QuantIronError) as ei:
+            a.upload_async(np.zeros(2 << n).ctypes.data, 1 << n)
+        assert ei.value.variant == "InvalidInputValue"
+    assert np.array_equal(out_a.numpy().view(np.complex128), sync_a)
+    assert np.array_equal(out_b.numpy().view(np.complex128), sync_b)
+    tol = 0 if prec == 0 else 1e-6
+    ref_b = w.reshape(2, -1)[::-1].reshape(-1)   # X on the top qubit swaps the halves
+    assert np.max(np.abs(sync_b - ref_b)) <= tol + 1e-15
+
+
+def qi_gate_row(qi, kind, targets):
+    from quant_iron_gb300 import workloads
+    return workloads.GateList().add(kind, targets).array()[0]

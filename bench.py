@@ -116,6 +116,18 @@ def cpu_port_sample(n, gates, budget_gates, threads):
     return secs / budget_gates
 
 
+def replica_throughput(ms, world, steps, device="cuda"):
+    """Whole-job throughput of `world` replicas: each rank processed LAYERS x steps layers
+    in its own ms; the job took the slowest rank's time (all_reduce MAX)."""
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        t = torch.tensor([ms], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    return ms, world * LAYERS * steps / (ms / 1e3)
+
+
 def host_mem_gb():
     try:
         for line in open("/proc/meminfo"):
@@ -380,13 +392,8 @@ def main():
     barrier()
     launches = qi.launch_count() - l0
     clk = clocks.stop()
-    ms = ev0.elapsed_time(ev1)
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms, value = replica_throughput(ev0.elapsed_time(ev1), world, args.steps)
     ms_per_step = ms / args.steps
-    value = world * LAYERS * args.steps / (ms / 1e3)
 
     # per-op device times of one execution (events on the launching stream)
     st.set_plus()

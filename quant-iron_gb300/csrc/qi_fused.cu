@@ -13,6 +13,7 @@
 #include "qi_tile.cuh"
 
 #include <algorithm>
+#include <atomic>
 
 namespace qi {
 
@@ -175,10 +176,13 @@ static Status launch_simt_t(qi_state *s, const TileGeom &g, const void *d_mat) {
     using V2 = typename Cx<T>::V2;
     const size_t smem = (size_t)R * R * sizeof(V2) + 32 * sizeof(TileIterTab) + 2 * ((size_t)R << g.nb) * sizeof(V2);
     auto kern = k_fused_simt<T, K>;
-    static bool attr_set = false;   // per instantiation
-    if (!attr_set) {
+    static std::atomic<bool> attr_set[64];   // per instantiation and device
+    int dev = 0;
+    QI_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) return err(QI_ERR_UNSUPPORTED, dev, 64, "device ordinal");
+    if (!attr_set[dev].load()) {
         QI_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
-        attr_set = true;
+        attr_set[dev].store(true);
     }
     int per_sm = 0;
     QI_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kSimtThreads, smem));

@@ -47,6 +47,7 @@
 #include "qi_tile.cuh"
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 
 namespace qi {
@@ -859,14 +860,17 @@ template <int K, bool PAIR, bool ROT, bool PHASE>
 static Status launch_tc_t(qi_state *s, const TileGeom &g, const void *d_tc, const void *poly) {
     using C = TcCfg<K, PAIR>;
     static_assert(C::SMEM <= 232448, "shared memory per CTA");
-    static bool attr_set = false;
-    static int num_sms = 0;
-    if (!attr_set) {
-        QI_CUDA(cudaFuncSetAttribute(k_fused_tc<K, PAIR, ROT, PHASE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::SMEM));
-        int dev = 0;
-        QI_CUDA(cudaGetDevice(&dev));
+    // the shared-memory opt-in and the SM count are per device (state handles may live on several)
+    static std::atomic<int> num_sms_of[64];
+    int dev = 0;
+    QI_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) return err(QI_ERR_UNSUPPORTED, dev, 64, "device ordinal");
+    int num_sms = num_sms_of[dev].load();
+    if (num_sms == 0) {
+        QI_CUDA(cudaFuncSetAttribute(k_fused_tc<K, PAIR, ROT, PHASE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)C::SMEM));
         QI_CUDA(cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, dev));
-        attr_set = true;
+        num_sms_of[dev].store(num_sms);
     }
     uint64_t grid = PAIR ? g.ntiles / 2 : g.ntiles;   // one persistent CTA per SM
     if (grid > (uint64_t)num_sms) grid = (uint64_t)num_sms;

@@ -9,7 +9,9 @@
 //   lambda_{j-1} = U_j^dagger lambda_j
 // The three steps of a parametric gate are one kernel: each work item loads
 // its pair (or quad) of psi and lambda, writes both back un-applied and adds
-// the derivative products to per-block FP64 partial sums.
+// the derivative products to per-block FP64 partial sums.  Runs of single-qubit
+// gates share one such pass (k_adjoint_multi), and runs of fixed gates are
+// un-applied on both states by one fused plan of their inverses.
 #include "qi_internal.hpp"
 #include "qi_device.cuh"
 #include "qi_plan.hpp"
@@ -17,6 +19,7 @@
 #include <algorithm>
 #include <cmath>
 #include <complex>
+#include <memory>
 
 namespace qi {
 
@@ -113,11 +116,114 @@ __global__ void __launch_bounds__(256) k_adjoint(typename Cx<T>::V2 *psi, typena
     }
 }
 
-// Fixed-order sum of the partial slots, written to out[0..ncomp).
-__global__ void k_finalize_to(const double *partials, int nb, int ncomp, double *out) {
+// A group of single-qubit gates, consecutive in the reverse sweep, on at most kMultiQubits
+// distinct qubits with at most kMultiStages gates per qubit.  Gates on distinct qubits
+// commute (and commute with one another's derivatives), so the group is processed qubit by
+// qubit in ascending order, each qubit's gates in sweep order: a work item holds the 2^M
+// amplitudes of psi and lambda its qubits span and, gate after gate, un-applies U on psi,
+// accumulates Re(conj(lambda) dU psi) and un-applies U on lambda, all in registers.
+constexpr int kMultiQubits = 4, kMultiStages = 2, kMultiComps = kMultiQubits * kMultiStages;
+struct MultiParams {
+    uint64_t nwork;
+    int8_t pos[kMultiQubits];                     // the group's qubits, ascending (combo bit i <-> pos[i])
+    double uinv[kMultiQubits][kMultiStages][8];   // qubit i, stage s: U^dagger, 2x2 complex row-major
+    double d[kMultiQubits][kMultiStages][8];      // dU/dtheta (zero for a fixed gate or an unused stage)
+};
+
+// Shared-memory read the compiler may not hoist out of the work loop: the group's
+// matrices are re-read (broadcast) per work item instead of pinning 16 registers per gate.
+__device__ __forceinline__ float2 lds_fresh(const float2 *p) {
+    float2 v;
+    asm volatile("ld.shared.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "r"((uint32_t)__cvta_generic_to_shared(p)));
+    return v;
+}
+__device__ __forceinline__ double2 lds_fresh(const double2 *p) {
+    double2 v;
+    asm volatile("ld.shared.v2.f64 {%0, %1}, [%2];" : "=d"(v.x), "=d"(v.y) : "r"((uint32_t)__cvta_generic_to_shared(p)));
+    return v;
+}
+
+template <typename T, int M, int S>
+__global__ void __launch_bounds__(256, (1 << M) * sizeof(T) >= 64 ? 1 : 2) k_adjoint_multi(typename Cx<T>::V2 *psi, typename Cx<T>::V2 *lam,
+                                                          const __grid_constant__ MultiParams p, double *partials) {
+    using X = Cx<T>;
+    using V2 = typename X::V2;
+    constexpr int D = 1 << M;
+    __shared__ V2 s_u[M][S][4], s_d[M][S][4];   // uniform across the block: broadcast reads
+    if (threadIdx.x < 4 * M * S) {
+        const int g = threadIdx.x / (4 * S), st = (threadIdx.x >> 2) % S, i = threadIdx.x & 3;
+        s_u[g][st][i] = X::make((T)p.uinv[g][st][2 * i], (T)p.uinv[g][st][2 * i + 1]);
+        s_d[g][st][i] = X::make((T)p.d[g][st][2 * i], (T)p.d[g][st][2 * i + 1]);
+    }
+    __syncthreads();
+    uint64_t bitm[M];
+#pragma unroll
+    for (int i = 0; i < M; ++i) bitm[i] = 1ull << p.pos[i];
+    double acc[M * S];
+#pragma unroll
+    for (int g = 0; g < M * S; ++g) acc[g] = 0.0;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t w = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; w < p.nwork; w += stride) {
+        const uint64_t base = insert_zeros(w, p.pos, M);
+        V2 x[D], l[D];
+#pragma unroll
+        for (int c = 0; c < D; ++c) {
+            uint64_t o = base;
+#pragma unroll
+            for (int i = 0; i < M; ++i)
+                if ((c >> i) & 1) o |= bitm[i];
+            x[c] = psi[o];
+            l[c] = lam[o];
+        }
+#pragma unroll
+        for (int g = 0; g < M; ++g) {   // qubit pos[g] is combo bit g: compile-time pair indices
+#pragma unroll
+            for (int st = 0; st < S; ++st) {
+                const V2 u0 = lds_fresh(&s_u[g][st][0]), u1 = lds_fresh(&s_u[g][st][1]);
+                const V2 u2 = lds_fresh(&s_u[g][st][2]), u3 = lds_fresh(&s_u[g][st][3]);
+                const V2 e0 = lds_fresh(&s_d[g][st][0]), e1 = lds_fresh(&s_d[g][st][1]);
+                const V2 e2 = lds_fresh(&s_d[g][st][2]), e3 = lds_fresh(&s_d[g][st][3]);
+                T part = 0;
+#pragma unroll
+                for (int c = 0; c < D; ++c) {
+                    if ((c >> g) & 1) continue;
+                    const int c1 = c | (1 << g);
+                    const V2 x0 = x[c], x1 = x[c1], l0 = l[c], l1 = l[c1];
+                    const V2 xn0 = X::fma(u1, x1, X::mul(u0, x0)), xn1 = X::fma(u3, x1, X::mul(u2, x0));
+                    const V2 d0 = X::fma(e1, xn1, X::mul(e0, xn0));
+                    const V2 d1 = X::fma(e3, xn1, X::mul(e2, xn0));
+                    part += l0.x * d0.x + l0.y * d0.y + l1.x * d1.x + l1.y * d1.y;   // Re(conj(lambda) dU psi')
+                    x[c] = xn0;
+                    x[c1] = xn1;
+                    l[c] = X::fma(u1, l1, X::mul(u0, l0));
+                    l[c1] = X::fma(u3, l1, X::mul(u2, l0));
+                }
+                acc[g * S + st] += (double)part;
+            }
+        }
+#pragma unroll
+        for (int c = 0; c < D; ++c) {
+            uint64_t o = base;
+#pragma unroll
+            for (int i = 0; i < M; ++i)
+                if ((c >> i) & 1) o |= bitm[i];
+            psi[o] = x[c];
+            lam[o] = l[c];
+        }
+    }
+#pragma unroll
+    for (int g = 0; g < M * S; ++g) {
+        const double v = block_sum(acc[g]);
+        if (threadIdx.x == 0) partials[blockIdx.x * kMultiComps + g] = v;
+    }
+}
+
+// Fixed-order sum of the partial slots (block i, component c at partials[i * stride + c]),
+// written to out[0..ncomp).
+__global__ void k_finalize_to(const double *partials, int nb, int ncomp, int stride, double *out) {
     for (int c = 0; c < ncomp; ++c) {
         double acc = 0.0;
-        for (int i = threadIdx.x; i < nb; i += blockDim.x) acc += partials[i * 4 + c];
+        for (int i = threadIdx.x; i < nb; i += blockDim.x) acc += partials[i * stride + c];
         double r = block_sum(acc);
         if (threadIdx.x == 0) out[c] = r;
         __syncthreads();
@@ -210,13 +316,14 @@ extern "C" qi_status qi_adjoint_gradient(qi_state *s, const qi_gate *gates, int6
         if (!st.ok()) return publish(st);
         resolved[(size_t)j] = g;
     }
-    // forward sweep
+    // forward sweep; the reverse sweep's fixed-gate segments use the same options
+    qi_exec_options plan_opts = {QI_FUSION_GREEDY, 0, 0, 0};
+    if (forward_opts) plan_opts = *forward_opts;
     {
         qi_plan plan;
         plan.n = n;
         plan.prec = s->prec;
-        if (forward_opts) plan.opts = *forward_opts;
-        else plan.opts.fusion = QI_FUSION_GREEDY;
+        plan.opts = plan_opts;
         std::vector<Elem> elems;
         Status st = plan_elems_from_gates(n, gates, n_gates, theta, n_theta, elems);
         if (st.ok()) st = build_plan(&plan, elems);
@@ -240,11 +347,8 @@ extern "C" qi_status qi_adjoint_gradient(qi_state *s, const qi_gate *gates, int6
     Status st = ok_status();
     if (n_terms > 0) st = sumop_apply(lam, s, terms, n_terms);
     else e = cudaMemsetAsync(lam->amps, 0, lam->bytes(), s->stream);
-    // derivative slots
-    int64_t nslots = 0;
-    for (int64_t j = 0; j < n_gates; ++j)
-        for (int k = 0; k < 3; ++k)
-            if (gates[j].param_ids[k] >= 0) ++nslots;
+    // derivative slots (one per parameter of a gate; a gate group uses one per member)
+    const int64_t nslots = 3 * n_gates + kMultiComps;
     double *d_gres = nullptr;
     if (st.ok() && nslots > 0) {
         e = cudaMalloc(&d_gres, (size_t)nslots * sizeof(double));
@@ -253,9 +357,118 @@ extern "C" qi_status qi_adjoint_gradient(qi_state *s, const qi_gate *gates, int6
     std::vector<std::pair<int64_t, int32_t>> slot_param;   // slot -> parameter id
     int64_t slot = nslots;
     const bool f32 = s->prec == QI_F32;
-    for (int64_t j = n_gates - 1; j >= 0 && st.ok(); --j) {
+    auto n_params = [&](int64_t jj) {
+        int c = 0;
+        for (int k = 0; k < 3; ++k) c += resolved[(size_t)jj].param_ids[k] >= 0;
+        return c;
+    };
+    // a single-qubit, uncontrolled gate with at most one parameter can join a gate group
+    auto groupable = [&](int64_t jj) {
+        const GateMatrix &m = mats[(size_t)jj];
+        return !m.pauli && m.nt == 1 && m.controls.empty() && n_params(jj) <= 1;
+    };
+    std::vector<std::unique_ptr<qi_plan>> seg_plans;   // kept until the sweep has run
+    for (int64_t j = n_gates - 1; j >= 0 && st.ok();) {
+        // single-qubit gates, consecutive in reverse, on at most kMultiQubits qubits with at
+        // most kMultiStages gates each: one pass for the group
+        int qcount[64] = {0};
+        uint64_t qmask = 0;
+        int64_t jj = j;
+        const int max_q = f32 ? kMultiQubits : kMultiQubits - 1;   // FP64 x 16 amplitudes spills
+        for (; jj >= 0 && groupable(jj); --jj) {
+            const int q = mats[(size_t)jj].t[0];
+            if (!((qmask >> q) & 1ull) && __builtin_popcountll(qmask) == max_q) break;
+            if (qcount[q] == kMultiStages) break;
+            qmask |= 1ull << q;
+            ++qcount[q];
+        }
+        const int64_t gsize = j - jj;
+        if (gsize >= 2) {
+            MultiParams mp;
+            std::memset(&mp, 0, sizeof(mp));
+            const int M = __builtin_popcountll(qmask);
+            int S = 1, b_of[64];
+            for (int q = 0, i = 0; q < 64; ++q)
+                if ((qmask >> q) & 1ull) {
+                    mp.pos[i] = (int8_t)q;
+                    b_of[q] = i++;
+                    S = std::max(S, qcount[q]);
+                }
+            for (int i = 0; i < M; ++i)
+                for (int t = 0; t < kMultiStages; ++t) mp.uinv[i][t][0] = mp.uinv[i][t][6] = 1.0;   // identity
+            int used[64] = {0};
+            std::vector<std::pair<int, int32_t>> comp_param;   // component -> parameter id
+            for (int64_t k = j; k > jj && st.ok(); --k) {
+                const GateMatrix &gm = mats[(size_t)k];
+                const qi_gate &g = resolved[(size_t)k];
+                const int b = b_of[gm.t[0]], t = used[gm.t[0]]++;
+                inverse_matrix(gm, mp.uinv[b][t]);
+                for (int q = 0; q < 3; ++q)
+                    if (g.param_ids[q] >= 0) {
+                        st = derivative_matrix(n, g, q, mp.d[b][t]);
+                        comp_param.push_back({b * S + t, g.param_ids[q]});
+                    }
+            }
+            if (!st.ok()) break;
+            mp.nwork = 1ull << (n - M);
+            const uint64_t nb64 = (mp.nwork + 255) / 256;
+            const unsigned nb = (unsigned)std::max<uint64_t>(
+                1, std::min<uint64_t>(nb64, (uint64_t)kReduceBlocks * 4 / kMultiComps));
+#define QI_AM(T, MM, SS) k_adjoint_multi<T, MM, SS><<<nb, 256, 0, s->stream>>>( \
+                (Cx<T>::V2 *)s->amps, (Cx<T>::V2 *)lam->amps, mp, s->d_partials)
+#define QI_AM_S(T, MM) { if (S == 1) QI_AM(T, MM, 1); else QI_AM(T, MM, 2); }
+            if (f32) {
+                if (M == 1) QI_AM_S(float, 1) else if (M == 2) QI_AM_S(float, 2)
+                else if (M == 3) QI_AM_S(float, 3) else QI_AM_S(float, 4)
+            } else {
+                if (M == 1) QI_AM_S(double, 1) else if (M == 2) QI_AM_S(double, 2) else QI_AM_S(double, 3)
+            }
+#undef QI_AM_S
+#undef QI_AM
+            slot -= M * S;
+            k_finalize_to<<<1, 256, 0, s->stream>>>(s->d_partials, (int)nb, M * S, kMultiComps, d_gres + slot);
+            count_launch(2);
+            st = check_launch("k_adjoint_multi");
+            for (auto &cp : comp_param) slot_param.push_back({slot + cp.first, cp.second});
+            j = jj;
+            continue;
+        }
+        // fixed gates, consecutive in reverse: their inverses as one fused plan on psi and lambda
+        for (jj = j; jj >= 0 && n_params(jj) == 0; --jj) {}
+        if (j - jj >= 2 && plan_opts.fusion != QI_FUSION_NONE) {
+            std::vector<Elem> inv;
+            for (int64_t k = j; k > jj; --k) {
+                GateMatrix gi = mats[(size_t)k];
+                if (gi.pauli) {
+                    gi.alpha_re = -gi.alpha_re;
+                    gi.alpha_im = -gi.alpha_im;
+                    gi.normalise_after = false;
+                } else {
+                    if (gi.nt == 0) continue;
+                    inverse_matrix(mats[(size_t)k], gi.m);
+                }
+                inv.push_back(make_elem_from_gate(gi, (int)inv.size()));
+            }
+            if (inv.empty()) {   // identities only
+                j = jj;
+                continue;
+            }
+            std::unique_ptr<qi_plan> seg(new qi_plan());
+            seg->n = n;
+            seg->prec = s->prec;
+            seg->opts = plan_opts;
+            seg->opts.renorm_every = -1;   // lambda = H psi is not a unit vector
+            st = build_plan(seg.get(), inv);
+            if (st.ok()) st = upload_plan(seg.get());
+            if (st.ok()) st = plan_execute(seg.get(), s);
+            if (st.ok()) st = plan_execute(seg.get(), lam);
+            seg_plans.push_back(std::move(seg));
+            j = jj;
+            continue;
+        }
         const GateMatrix &gm = mats[(size_t)j];
         const qi_gate &g = resolved[(size_t)j];
+        --j;
         int ids[3], nd = 0;
         for (int k = 0; k < 3; ++k)
             if (g.param_ids[k] >= 0) ids[nd++] = k;
@@ -300,7 +513,7 @@ extern "C" qi_status qi_adjoint_gradient(qi_state *s, const qi_gate *gates, int6
             else k_adjoint<double, 2><<<nb, 256, 0, s->stream>>>((double2 *)s->amps, (double2 *)lam->amps, p, s->d_partials);
         }
         slot -= nd;
-        k_finalize_to<<<1, 256, 0, s->stream>>>(s->d_partials, (int)nb, nd, d_gres + slot);
+        k_finalize_to<<<1, 256, 0, s->stream>>>(s->d_partials, (int)nb, nd, 4, d_gres + slot);
         count_launch(2);
         st = check_launch("k_adjoint");
         for (int q = 0; q < nd; ++q) slot_param.push_back({slot + q, g.param_ids[ids[q]]});
@@ -314,8 +527,12 @@ extern "C" qi_status qi_adjoint_gradient(qi_state *s, const qi_gate *gates, int6
         if (e != cudaSuccess) st = cuda_status(e, "adjoint");
         for (auto &sp : slot_param) grads_out[sp.second] += 2.0 * h[(size_t)sp.first];
     }
-    if (d_gres) cudaFree(d_gres);
     cudaStreamSynchronize(s->stream);
+    for (auto &sp : seg_plans) {
+        if (sp->d_mats) cudaFree(sp->d_mats);
+        if (sp->d_tc) cudaFree(sp->d_tc);
+    }
+    if (d_gres) cudaFree(d_gres);
     qi_state_destroy(lam);
     return publish(st);
 }

@@ -42,7 +42,7 @@ namespace qi {
 using cd = std::complex<double>;
 
 // ------------------------------------------------------------ elements ---
-static Elem make_elem_from_gate(const GateMatrix &gm, int src) {
+Elem make_elem_from_gate(const GateMatrix &gm, int src) {
     Elem e;
     e.src = src;
     e.gm = gm;

@@ -61,4 +61,6 @@ std::vector<Block> choose_partition(qi_plan *p, const std::vector<Elem> &elems, 
 // false when no trained model is loaded.  *ms_out = predicted device time of the chosen plan.
 bool learned_choice(qi_plan *p, const std::vector<Elem> &elems, int kmax, int *k_out, int *tc_out, double *ms_out);
 Elem pauli_exp_elem(const qi_pauli_term &t, double far, double fai, int src);
+// Plan element of one gate matrix (support, diagonal and fusable flags).
+Elem make_elem_from_gate(const GateMatrix &gm, int src);
 }  // namespace qi

@@ -111,3 +111,75 @@ def test_adjoint_26q_fp32_vs_fp64_gpu(qi):
     rel = np.linalg.norm(grads[1][1] - grads[0][1]) / np.linalg.norm(grads[0][1])
     assert rel < 1e-4, rel
     assert abs(grads[1][0] - grads[0][0]) < 1e-4
+
+
+def grouped_sweep_circuit(n, n_runs, seed):
+    """Alternating runs for the reverse sweep's three paths: single-qubit runs (parametric
+    and fixed gates, one to three gates on the same qubit in a row, so groups split on a
+    fifth qubit and on a third gate per qubit), fixed runs (CNOT, SWAP, Toffoli, H, Pauli
+    evolutions) un-applied as one fused plan, and lone controlled or two-parameter gates
+    on the per-gate path.  Parameter ids are shared now and then."""
+    rng = np.random.default_rng(seed)
+    gl = workloads.GateList()
+    npar = 0
+    for _ in range(n_runs):
+        for _ in range(int(rng.integers(3, 12))):
+            q = int(rng.integers(0, n))
+            for _ in range(int(rng.integers(1, 4))):
+                kind = str(rng.choice(["RX", "RY", "RZ", "P", "H", "T", "SDAG"]))
+                if kind in workloads.PARAMETRIC:
+                    pid = npar if rng.random() < 0.85 or npar == 0 else int(rng.integers(0, npar))
+                    npar = max(npar, pid + 1)
+                    gl.add(kind, [q], [], [0.0], [pid])
+                else:
+                    gl.add(kind, [q])
+        for _ in range(int(rng.integers(2, 8))):
+            r = rng.random()
+            a, b, c = (int(x) for x in rng.choice(n, 3, replace=False))
+            if r < 0.4:
+                gl.add("CNOT", [b], [a])
+            elif r < 0.55:
+                gl.add("SWAP", [a, b])
+            elif r < 0.65:
+                gl.add("TOFFOLI", [c], [a, b])
+            elif r < 0.8:
+                gl.add("H", [a])
+            else:
+                gl.add("PAULI_EVOLUTION", [], [], [rng.uniform(-1, 1), 0.0, 0.3], xmask=(1 << a) | (1 << b),
+                       zmask=(1 << b) | (1 << c))
+        if rng.random() < 0.5:
+            a, b = (int(x) for x in rng.choice(n, 2, replace=False))
+            gl.add("RY", [a], [b], [0.0], [npar])
+            npar += 1
+        else:
+            gl.add("RYPHASE", [int(rng.integers(0, n))], [], [0.0, 0.0], [npar, npar + 1])
+            npar += 2
+    theta = rng.uniform(-np.pi, np.pi, size=npar)
+    return gl.array(), theta
+
+
+@pytest.mark.parametrize("n", [9, 12])
+def test_grouped_reverse_sweep_vs_per_gate_and_fd(qi, orc, n):
+    """Single-qubit groups and fused fixed runs in the reverse sweep: FP64 gradients equal
+    the per-gate sweep (fusion off) to 1e-10, match FP64 finite differences of the oracle
+    to 1e-6 on a seeded subset, FP32 stays within 1e-4 of FP64, and both sweeps restore
+    the initial state."""
+    gates, theta = grouped_sweep_circuit(n, 6, seed=n)
+    terms = workloads.xxz_periodic(n, seed=2)
+    init = workloads.plus_state(n)
+    res = {}
+    for prec, fusion in ((0, qi.FUSION_NONE), (0, qi.FUSION_GREEDY), (1, qi.FUSION_GREEDY)):
+        with qi.DeviceState(n, prec) as st:
+            st.upload(init)
+            e, g = qi.adjoint_gradient(st, gates, theta, terms, fusion=fusion)
+            back = st.download()
+        assert np.max(np.abs(back - init)) < (1e-12 if prec == 0 else 1e-5)
+        res[(prec, fusion)] = (e, g)
+    g_none, g64 = res[(0, qi.FUSION_NONE)][1], res[(0, qi.FUSION_GREEDY)][1]
+    assert np.linalg.norm(g64 - g_none) / np.linalg.norm(g_none) < 1e-10
+    g32 = res[(1, qi.FUSION_GREEDY)][1]
+    assert np.linalg.norm(g32 - g64) / np.linalg.norm(g64) < 1e-4
+    rng = np.random.default_rng(5)
+    ids = sorted(int(x) for x in rng.choice(theta.size, min(12, theta.size), replace=False))
+    g_ref = fd_grad(orc, n, gates, theta, terms, init, ids)
+    assert np.linalg.norm(g64[ids] - g_ref) / np.linalg.norm(g_ref) < 1e-6

@@ -43,7 +43,7 @@ def parse():
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
     ap.add_argument("--qubits", type=int, default=N_QUBITS)
     ap.add_argument("--skip-baselines", action="store_true", help="skip FP64/FP32 per-gate and CPU legs")
-    ap.add_argument("--profile-case", default=None, choices=["fused26", "trotter26"],
+    ap.add_argument("--profile-case", default=None, choices=["fused26", "trotter26", "adjoint26"],
                     help="run a small fixed case for ncu captures instead of the benchmark")
     return ap.parse_args()
 
@@ -329,6 +329,25 @@ def profile_case_trotter26():
         st.close()
 
 
+def profile_case_adjoint26():
+    """Small case for ncu (26 qubits FP32 = 512 MB per state): one adjoint gradient of the
+    26-qubit hardware-efficient ansatz (12 layers, 624 parameters) on the periodic XXZ
+    energy — forward plan, <H>, lambda = H psi, then the grouped reverse sweep
+    (k_adjoint_multi, fused inverse plans of the CNOT ladders)."""
+    import __graft_entry__ as ge
+    qi = ge.load_package()
+    from quant_iron_gb300 import workloads
+    n = 26
+    import numpy as np
+    gates, theta = workloads.hea_ansatz(n, 12, seed=1)
+    terms = workloads.xxz_periodic(n, seed=1)
+    st = qi.DeviceState(n, qi.F32)
+    st.set_zero()
+    e, g = qi.adjoint_gradient(st, gates, theta, terms)
+    st.synchronize()
+    print("profile case done, E = %.9f, |grad| = %.9f" % (e, float(np.linalg.norm(g))))
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -339,6 +358,9 @@ def main():
         return
     if args.profile_case == "trotter26":
         profile_case_trotter26()
+        return
+    if args.profile_case == "adjoint26":
+        profile_case_adjoint26()
         return
     import numpy as np
     import torch

@@ -15,8 +15,10 @@
 #include "qi_internal.hpp"
 #include "qi_device.cuh"
 #include "qi_plan.hpp"
+#include "qi_tile.cuh"
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <complex>
 #include <memory>
@@ -120,102 +122,333 @@ __global__ void __launch_bounds__(256) k_adjoint(typename Cx<T>::V2 *psi, typena
 // distinct qubits with at most kMultiStages gates per qubit.  Gates on distinct qubits
 // commute (and commute with one another's derivatives), so the group is processed qubit by
 // qubit in ascending order, each qubit's gates in sweep order: a work item holds the 2^M
-// amplitudes of psi and lambda its qubits span and, gate after gate, un-applies U on psi,
-// accumulates Re(conj(lambda) dU psi) and un-applies U on lambda, all in registers.
+// amplitudes of psi and lambda its qubits span and, gate after gate, adds
+// Re(conj(lambda) D psi) with D = dU U^dagger (the derivative taken before un-applying),
+// then un-applies U^dagger on psi and on lambda, all in registers.
 constexpr int kMultiQubits = 4, kMultiStages = 2, kMultiComps = kMultiQubits * kMultiStages;
+// Stage kinds: matrix structure of U^dagger and D together (host-classified, exact zeros).
+enum : int8_t { kStageGeneral = 0, kStageDiag = 1, kStageReal = 2, kStageNoDeriv = 4 };
 struct MultiParams {
     uint64_t nwork;
     int8_t pos[kMultiQubits];                     // the group's qubits, ascending (combo bit i <-> pos[i])
+    int8_t kind[kMultiQubits][kMultiStages];      // kStage* (| kStageNoDeriv when D = 0)
     double uinv[kMultiQubits][kMultiStages][8];   // qubit i, stage s: U^dagger, 2x2 complex row-major
-    double d[kMultiQubits][kMultiStages][8];      // dU/dtheta (zero for a fixed gate or an unused stage)
+    double d[kMultiQubits][kMultiStages][8];      // D = dU/dtheta U^dagger (zero for a fixed gate / unused stage)
 };
 
-// Shared-memory read the compiler may not hoist out of the work loop: the group's
-// matrices are re-read (broadcast) per work item instead of pinning 16 registers per gate.
-__device__ __forceinline__ float2 lds_fresh(const float2 *p) {
-    float2 v;
-    asm volatile("ld.shared.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "r"((uint32_t)__cvta_generic_to_shared(p)));
-    return v;
+// Launch shape per precision: threads per block and cp.async buffers (the copies of the
+// next kPipe - 1 work items are in flight while one is computed).  Both fill ~192 KB of
+// shared memory with one block per SM.
+template <typename T> struct MultiShape;
+template <> struct MultiShape<float> { static constexpr int kThreads = 384, kPipe = 2; using Amp = uint64_t; };
+template <> struct MultiShape<double> { static constexpr int kThreads = 256, kPipe = 3; using Amp = double2; };
+
+// ---- FP32: an amplitude is one 64-bit register pair (re, im), arithmetic in packed f32x2.
+__device__ __forceinline__ uint64_t pk2(float a, float b) {
+    uint64_t r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+    return r;
 }
-__device__ __forceinline__ double2 lds_fresh(const double2 *p) {
-    double2 v;
-    asm volatile("ld.shared.v2.f64 {%0, %1}, [%2];" : "=d"(v.x), "=d"(v.y) : "r"((uint32_t)__cvta_generic_to_shared(p)));
-    return v;
+__device__ __forceinline__ float2 upk2(uint64_t v) {
+    float2 r;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(r.x), "=f"(r.y) : "l"(v));
+    return r;
+}
+__device__ __forceinline__ uint64_t mul2(uint64_t a, uint64_t b) {
+    uint64_t d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ uint64_t fma2(uint64_t a, uint64_t b, uint64_t c) {
+    uint64_t d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+__device__ __forceinline__ uint64_t swap2(uint64_t v) {
+    const float2 f = upk2(v);
+    return pk2(f.y, f.x);
+}
+// Stage table: entry k of a 2x2 complex matrix (a + ib) as A = (a, a) and B = (-b, b), so
+// that (a + ib) x = A * x + B * swap(x) lane-wise; T[0..7] = U^dagger, T[8..15] = D.
+__device__ __forceinline__ void build_stage_table(uint64_t *T, const double *u, const double *d) {
+    for (int k = 0; k < 4; ++k) {
+        T[2 * k] = pk2((float)u[2 * k], (float)u[2 * k]);
+        T[2 * k + 1] = pk2((float)-u[2 * k + 1], (float)u[2 * k + 1]);
+        T[8 + 2 * k] = pk2((float)d[2 * k], (float)d[2 * k]);
+        T[8 + 2 * k + 1] = pk2((float)-d[2 * k + 1], (float)d[2 * k + 1]);
+    }
 }
 
-template <typename T, int M, int S>
-__global__ void __launch_bounds__(256, (1 << M) * sizeof(T) >= 64 ? 1 : 2) k_adjoint_multi(typename Cx<T>::V2 *psi, typename Cx<T>::V2 *lam,
-                                                          const __grid_constant__ MultiParams p, double *partials) {
-    using X = Cx<T>;
-    using V2 = typename X::V2;
-    constexpr int D = 1 << M;
-    __shared__ V2 s_u[M][S][4], s_d[M][S][4];   // uniform across the block: broadcast reads
-    if (threadIdx.x < 4 * M * S) {
-        const int g = threadIdx.x / (4 * S), st = (threadIdx.x >> 2) % S, i = threadIdx.x & 3;
-        s_u[g][st][i] = X::make((T)p.uinv[g][st][2 * i], (T)p.uinv[g][st][2 * i + 1]);
-        s_d[g][st][i] = X::make((T)p.d[g][st][2 * i], (T)p.d[g][st][2 * i + 1]);
+// One stage (gate) on combo bit G: derivative term Re(conj(lambda) D psi), then un-apply.
+template <int D, int G>
+__device__ __forceinline__ float multi_stage_f32(uint64_t *x, uint64_t *l, int kind, const uint64_t *T) {
+    uint64_t acc = 0;   // lane-wise partial sums (+0.0f, +0.0f)
+    const bool deriv = !(kind & kStageNoDeriv);
+    kind &= 3;
+    if (kind == kStageDiag) {
+        const uint64_t A0 = T[0], B0 = T[1], A3 = T[6], B3 = T[7], P0 = T[8], Q0 = T[9], P3 = T[14], Q3 = T[15];
+#pragma unroll
+        for (int c = 0; c < D; ++c) {
+            if ((c >> G) & 1) continue;
+            const int c1 = c | (1 << G);
+            const uint64_t x0 = x[c], x1 = x[c1], l0 = l[c], l1 = l[c1];
+            const uint64_t x0s = swap2(x0), x1s = swap2(x1);
+            if (deriv) {   // Re(delta conj(l) x) = (l * (dr, dr)) . x + (l * (-di, di)) . swap(x)
+                acc = fma2(mul2(l0, P0), x0, acc);
+                acc = fma2(mul2(l0, Q0), x0s, acc);
+                acc = fma2(mul2(l1, P3), x1, acc);
+                acc = fma2(mul2(l1, Q3), x1s, acc);
+            }
+            x[c] = fma2(B0, x0s, mul2(A0, x0));
+            x[c1] = fma2(B3, x1s, mul2(A3, x1));
+            l[c] = fma2(B0, swap2(l0), mul2(A0, l0));
+            l[c1] = fma2(B3, swap2(l1), mul2(A3, l1));
+        }
+    } else if (kind == kStageReal) {
+        const uint64_t R0 = T[0], R1 = T[2], R2 = T[4], R3 = T[6], Q0 = T[8], Q1 = T[10], Q2 = T[12], Q3 = T[14];
+#pragma unroll
+        for (int c = 0; c < D; ++c) {
+            if ((c >> G) & 1) continue;
+            const int c1 = c | (1 << G);
+            const uint64_t x0 = x[c], x1 = x[c1], l0 = l[c], l1 = l[c1];
+            if (deriv) {
+                acc = fma2(l0, fma2(Q1, x1, mul2(Q0, x0)), acc);
+                acc = fma2(l1, fma2(Q3, x1, mul2(Q2, x0)), acc);
+            }
+            x[c] = fma2(R1, x1, mul2(R0, x0));
+            x[c1] = fma2(R3, x1, mul2(R2, x0));
+            l[c] = fma2(R1, l1, mul2(R0, l0));
+            l[c1] = fma2(R3, l1, mul2(R2, l0));
+        }
+    } else {
+#pragma unroll
+        for (int c = 0; c < D; ++c) {
+            if ((c >> G) & 1) continue;
+            const int c1 = c | (1 << G);
+            const uint64_t x0 = x[c], x1 = x[c1], l0 = l[c], l1 = l[c1];
+            const uint64_t x0s = swap2(x0), x1s = swap2(x1), l0s = swap2(l0), l1s = swap2(l1);
+            if (deriv) {
+                const uint64_t d0 = fma2(T[11], x1s, fma2(T[10], x1, fma2(T[9], x0s, mul2(T[8], x0))));
+                const uint64_t d1 = fma2(T[15], x1s, fma2(T[14], x1, fma2(T[13], x0s, mul2(T[12], x0))));
+                acc = fma2(l0, d0, acc);
+                acc = fma2(l1, d1, acc);
+            }
+            x[c] = fma2(T[3], x1s, fma2(T[2], x1, fma2(T[1], x0s, mul2(T[0], x0))));
+            x[c1] = fma2(T[7], x1s, fma2(T[6], x1, fma2(T[5], x0s, mul2(T[4], x0))));
+            l[c] = fma2(T[3], l1s, fma2(T[2], l1, fma2(T[1], l0s, mul2(T[0], l0))));
+            l[c1] = fma2(T[7], l1s, fma2(T[6], l1, fma2(T[5], l0s, mul2(T[4], l0))));
+        }
     }
+    const float2 a = upk2(acc);
+    return a.x + a.y;
+}
+
+// ---- FP64: double2 amplitudes, plain complex arithmetic.
+template <int D, int G>
+__device__ __forceinline__ double multi_stage_f64(double2 *x, double2 *l, int kind, const double2 *u,
+                                                  const double2 *e) {
+    using X = Cx<double>;
+    double part = 0;
+    const bool deriv = !(kind & kStageNoDeriv);
+    kind &= 3;
+    if (kind == kStageDiag) {
+        const double2 u0 = u[0], u3 = u[3], e0 = e[0], e3 = e[3];
+#pragma unroll
+        for (int c = 0; c < D; ++c) {
+            if ((c >> G) & 1) continue;
+            const int c1 = c | (1 << G);
+            if (deriv) {
+                const double2 d0 = X::mul(e0, x[c]), d1 = X::mul(e3, x[c1]);
+                part += l[c].x * d0.x + l[c].y * d0.y + l[c1].x * d1.x + l[c1].y * d1.y;
+            }
+            x[c] = X::mul(u0, x[c]);
+            x[c1] = X::mul(u3, x[c1]);
+            l[c] = X::mul(u0, l[c]);
+            l[c1] = X::mul(u3, l[c1]);
+        }
+    } else {   // real matrices take the general form: FP64 states are bound by the FP64 pipe either way
+        const double2 u0 = u[0], u1 = u[1], u2 = u[2], u3 = u[3];
+        const double2 e0 = e[0], e1 = e[1], e2 = e[2], e3 = e[3];
+#pragma unroll
+        for (int c = 0; c < D; ++c) {
+            if ((c >> G) & 1) continue;
+            const int c1 = c | (1 << G);
+            const double2 x0 = x[c], x1 = x[c1], l0 = l[c], l1 = l[c1];
+            if (deriv) {
+                const double2 d0 = X::fma(e1, x1, X::mul(e0, x0)), d1 = X::fma(e3, x1, X::mul(e2, x0));
+                part += l0.x * d0.x + l0.y * d0.y + l1.x * d1.x + l1.y * d1.y;
+            }
+            x[c] = X::fma(u1, x1, X::mul(u0, x0));
+            x[c1] = X::fma(u3, x1, X::mul(u2, x0));
+            l[c] = X::fma(u1, l1, X::mul(u0, l0));
+            l[c1] = X::fma(u3, l1, X::mul(u2, l0));
+        }
+    }
+    return part;
+}
+
+// Per-block stage data in shared memory.
+template <typename T, int M, int S> struct MultiStageSmem;
+template <int M, int S> struct MultiStageSmem<float, M, S> {
+    uint64_t tab[M][S][16];
+    int8_t kind[M][S];
+    __device__ void load(const MultiParams &p) {
+        if (threadIdx.x < M * S) {
+            const int g = threadIdx.x / S, st = threadIdx.x % S;
+            build_stage_table(tab[g][st], p.uinv[g][st], p.d[g][st]);
+            kind[g][st] = p.kind[g][st];
+        }
+    }
+    template <int G> __device__ __forceinline__ float run(uint64_t *x, uint64_t *l, int st) const {
+        return multi_stage_f32<1 << M, G>(x, l, kind[G][st], tab[G][st]);
+    }
+};
+template <int M, int S> struct MultiStageSmem<double, M, S> {
+    double2 u[M][S][4], e[M][S][4];
+    int8_t kind[M][S];
+    __device__ void load(const MultiParams &p) {
+        if (threadIdx.x < 4 * M * S) {
+            const int g = threadIdx.x / (4 * S), st = (threadIdx.x >> 2) % S, i = threadIdx.x & 3;
+            u[g][st][i] = make_double2(p.uinv[g][st][2 * i], p.uinv[g][st][2 * i + 1]);
+            e[g][st][i] = make_double2(p.d[g][st][2 * i], p.d[g][st][2 * i + 1]);
+            if (i == 0) kind[g][st] = p.kind[g][st];
+        }
+    }
+    template <int G> __device__ __forceinline__ double run(double2 *x, double2 *l, int st) const {
+        return multi_stage_f64<1 << M, G>(x, l, kind[G][st], u[G][st], e[G][st]);
+    }
+};
+
+template <typename T, int M, int S, int G, typename Amp, typename Acc>
+__device__ __forceinline__ void multi_qubits(Amp *x, Amp *l, const MultiStageSmem<T, M, S> &sm, Acc *acc) {
+    if constexpr (G < M) {
+#pragma unroll
+        for (int st = 0; st < S; ++st) acc[G * S + st] += sm.template run<G>(x, l, st);
+        multi_qubits<T, M, S, G + 1>(x, l, sm, acc);
+    }
+}
+
+// Work items stream through shared memory: each thread copies its item's 2^M amplitudes of
+// psi and lambda with cp.async kPipe - 1 items ahead (the copies hold no registers while in
+// flight), then reads them back, runs the stages and stores to global memory.  Thread t owns
+// column t of every buffer, so no block barrier is needed in the loop.  FP32 derivative
+// terms are summed in FP32 over batches of 16 items per thread and folded into FP64 per batch (an
+// FP64 add per item and stage would load the scarce FP64 pipe).
+template <typename T, int M, int S>
+__global__ void __launch_bounds__(MultiShape<T>::kThreads, 1)
+    k_adjoint_multi(typename MultiShape<T>::Amp *psi, typename MultiShape<T>::Amp *lam,
+                    const __grid_constant__ MultiParams p, double *partials) {
+    using Amp = typename MultiShape<T>::Amp;
+    constexpr int TH = MultiShape<T>::kThreads, PIPE = MultiShape<T>::kPipe, D = 1 << M;
+    constexpr int BATCH = sizeof(T) == 4 ? 16 : 1;
+    extern __shared__ __align__(16) unsigned char multi_smem[];
+    Amp *buf = reinterpret_cast<Amp *>(multi_smem);   // [PIPE][2][D][TH]
+    __shared__ MultiStageSmem<T, M, S> sm;
+    sm.load(p);
     __syncthreads();
     uint64_t bitm[M];
 #pragma unroll
     for (int i = 0; i < M; ++i) bitm[i] = 1ull << p.pos[i];
-    double acc[M * S];
+    const int t = threadIdx.x;
+    auto slot = [&](int stage, int which, int c) -> Amp * {
+        return buf + (((size_t)stage * 2 + which) * D + c) * TH + t;
+    };
+    auto issue = [&](uint64_t w, int stage) {
+        if (w < p.nwork) {
+            const uint64_t base = insert_zeros(w, p.pos, M);
 #pragma unroll
-    for (int g = 0; g < M * S; ++g) acc[g] = 0.0;
-    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t w = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; w < p.nwork; w += stride) {
-        const uint64_t base = insert_zeros(w, p.pos, M);
-        V2 x[D], l[D];
+            for (int c = 0; c < D; ++c) {
+                uint64_t o = base;
 #pragma unroll
-        for (int c = 0; c < D; ++c) {
-            uint64_t o = base;
-#pragma unroll
-            for (int i = 0; i < M; ++i)
-                if ((c >> i) & 1) o |= bitm[i];
-            x[c] = psi[o];
-            l[c] = lam[o];
-        }
-#pragma unroll
-        for (int g = 0; g < M; ++g) {   // qubit pos[g] is combo bit g: compile-time pair indices
-#pragma unroll
-            for (int st = 0; st < S; ++st) {
-                const V2 u0 = lds_fresh(&s_u[g][st][0]), u1 = lds_fresh(&s_u[g][st][1]);
-                const V2 u2 = lds_fresh(&s_u[g][st][2]), u3 = lds_fresh(&s_u[g][st][3]);
-                const V2 e0 = lds_fresh(&s_d[g][st][0]), e1 = lds_fresh(&s_d[g][st][1]);
-                const V2 e2 = lds_fresh(&s_d[g][st][2]), e3 = lds_fresh(&s_d[g][st][3]);
-                T part = 0;
-#pragma unroll
-                for (int c = 0; c < D; ++c) {
-                    if ((c >> g) & 1) continue;
-                    const int c1 = c | (1 << g);
-                    const V2 x0 = x[c], x1 = x[c1], l0 = l[c], l1 = l[c1];
-                    const V2 xn0 = X::fma(u1, x1, X::mul(u0, x0)), xn1 = X::fma(u3, x1, X::mul(u2, x0));
-                    const V2 d0 = X::fma(e1, xn1, X::mul(e0, xn0));
-                    const V2 d1 = X::fma(e3, xn1, X::mul(e2, xn0));
-                    part += l0.x * d0.x + l0.y * d0.y + l1.x * d1.x + l1.y * d1.y;   // Re(conj(lambda) dU psi')
-                    x[c] = xn0;
-                    x[c1] = xn1;
-                    l[c] = X::fma(u1, l1, X::mul(u0, l0));
-                    l[c1] = X::fma(u3, l1, X::mul(u2, l0));
+                for (int i = 0; i < M; ++i)
+                    if ((c >> i) & 1) o |= bitm[i];
+                if constexpr (sizeof(Amp) == 8) {
+                    cp_async_8(slot(stage, 0, c), psi + o);
+                    cp_async_8(slot(stage, 1, c), lam + o);
+                } else {
+                    cp_async_16(slot(stage, 0, c), psi + o);
+                    cp_async_16(slot(stage, 1, c), lam + o);
                 }
-                acc[g * S + st] += (double)part;
             }
         }
+        cp_async_commit();   // an empty group past the end keeps the group count uniform
+    };
+    double acc[M * S];
+    T accb[M * S];
 #pragma unroll
-        for (int c = 0; c < D; ++c) {
-            uint64_t o = base;
+    for (int g = 0; g < M * S; ++g) acc[g] = 0.0;
+    const uint64_t stride = (uint64_t)gridDim.x * TH;
+    const uint64_t w0 = blockIdx.x * (uint64_t)TH + t;
 #pragma unroll
-            for (int i = 0; i < M; ++i)
-                if ((c >> i) & 1) o |= bitm[i];
-            psi[o] = x[c];
-            lam[o] = l[c];
+    for (int k = 0; k < PIPE - 1; ++k) issue(w0 + k * stride, k);
+    int stage = 0;
+    for (uint64_t wb = w0; wb < p.nwork; wb += BATCH * stride) {
+        const uint64_t wend = min(p.nwork, wb + BATCH * stride);
+#pragma unroll
+        for (int g = 0; g < M * S; ++g) accb[g] = 0;
+#pragma unroll 1
+        for (uint64_t w = wb; w < wend; w += stride) {
+            cp_async_wait<PIPE - 2>();   // this item's group has landed
+            Amp x[D], l[D];
+#pragma unroll
+            for (int c = 0; c < D; ++c) {
+                x[c] = *slot(stage, 0, c);
+                l[c] = *slot(stage, 1, c);
+            }
+            // refill the buffer read one iteration ago (only this thread uses its column)
+            issue(w + (PIPE - 1) * stride, stage == 0 ? PIPE - 1 : stage - 1);
+            multi_qubits<T, M, S, 0>(x, l, sm, accb);
+            const uint64_t base = insert_zeros(w, p.pos, M);
+#pragma unroll
+            for (int c = 0; c < D; ++c) {
+                uint64_t o = base;
+#pragma unroll
+                for (int i = 0; i < M; ++i)
+                    if ((c >> i) & 1) o |= bitm[i];
+                psi[o] = x[c];
+                lam[o] = l[c];
+            }
+            stage = stage == PIPE - 1 ? 0 : stage + 1;
         }
+#pragma unroll
+        for (int g = 0; g < M * S; ++g) acc[g] += (double)accb[g];
     }
+    cp_async_wait<0>();
 #pragma unroll
     for (int g = 0; g < M * S; ++g) {
         const double v = block_sum(acc[g]);
         if (threadIdx.x == 0) partials[blockIdx.x * kMultiComps + g] = v;
     }
+}
+
+// One block per SM slot the shared-memory pipeline leaves (grid-stride over the work items);
+// *nb_out = blocks launched (= partial-sum rows).
+template <typename T, int M, int S>
+static Status launch_adjoint_multi(qi_state *s, qi_state *lam, const MultiParams &mp, unsigned *nb_out) {
+    using Amp = typename MultiShape<T>::Amp;
+    constexpr int TH = MultiShape<T>::kThreads;
+    const size_t smem = (size_t)MultiShape<T>::kPipe * 2 * (1 << M) * TH * sizeof(Amp);
+    auto kern = k_adjoint_multi<T, M, S>;
+    static std::atomic<int> per_sm_of[64];   // per instantiation and device: blocks per SM, 0 = not set up
+    static std::atomic<int> sms_of[64];
+    int dev = 0;
+    QI_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) return err(QI_ERR_UNSUPPORTED, dev, 64, "device ordinal");
+    if (per_sm_of[dev].load() == 0) {
+        QI_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        int per_sm = 0, sms = 0;
+        QI_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, TH, smem));
+        QI_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        sms_of[dev].store(std::max(sms, 1));
+        per_sm_of[dev].store(std::max(per_sm, 1));
+    }
+    const uint64_t want = (mp.nwork + TH - 1) / TH;
+    const uint64_t cap = std::min<uint64_t>((uint64_t)sms_of[dev].load() * per_sm_of[dev].load(),
+                                            (uint64_t)kReduceBlocks * 4 / kMultiComps);
+    const unsigned nb = (unsigned)std::max<uint64_t>(1, std::min(want, cap));
+    kern<<<nb, TH, smem, s->stream>>>((Amp *)s->amps, (Amp *)lam->amps, mp, s->d_partials);
+    *nb_out = nb;
+    return check_launch("k_adjoint_multi");
 }
 
 // Fixed-order sum of the partial slots (block i, component c at partials[i * stride + c]),
@@ -395,27 +628,52 @@ extern "C" qi_status qi_adjoint_gradient(qi_state *s, const qi_gate *gates, int6
                     S = std::max(S, qcount[q]);
                 }
             for (int i = 0; i < M; ++i)
-                for (int t = 0; t < kMultiStages; ++t) mp.uinv[i][t][0] = mp.uinv[i][t][6] = 1.0;   // identity
+                for (int t = 0; t < kMultiStages; ++t) {
+                    mp.uinv[i][t][0] = mp.uinv[i][t][6] = 1.0;   // identity, no derivative
+                    mp.kind[i][t] = kStageDiag | kStageNoDeriv;
+                }
             int used[64] = {0};
             std::vector<std::pair<int, int32_t>> comp_param;   // component -> parameter id
             for (int64_t k = j; k > jj && st.ok(); --k) {
                 const GateMatrix &gm = mats[(size_t)k];
                 const qi_gate &g = resolved[(size_t)k];
                 const int b = b_of[gm.t[0]], t = used[gm.t[0]]++;
-                inverse_matrix(gm, mp.uinv[b][t]);
+                double *ui = mp.uinv[b][t], *dd = mp.d[b][t];
+                inverse_matrix(gm, ui);
+                double dU[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+                bool has_d = false;
                 for (int q = 0; q < 3; ++q)
                     if (g.param_ids[q] >= 0) {
-                        st = derivative_matrix(n, g, q, mp.d[b][t]);
+                        st = derivative_matrix(n, g, q, dU);
                         comp_param.push_back({b * S + t, g.param_ids[q]});
+                        has_d = true;
                     }
+                // D = dU U^dagger: the derivative term on psi before it is un-applied
+                for (int r = 0; r < 2; ++r)
+                    for (int c = 0; c < 2; ++c) {
+                        double re = 0, im = 0;
+                        for (int m = 0; m < 2; ++m) {
+                            const double ar = dU[2 * (2 * r + m)], ai = dU[2 * (2 * r + m) + 1];
+                            const double br = ui[2 * (2 * m + c)], bi = ui[2 * (2 * m + c) + 1];
+                            re += ar * br - ai * bi;
+                            im += ar * bi + ai * br;
+                        }
+                        dd[2 * (2 * r + c)] = re;
+                        dd[2 * (2 * r + c) + 1] = im;
+                    }
+                bool diag = true, real = true;
+                for (int e = 0; e < 8; ++e) {
+                    const bool off = e == 2 || e == 3 || e == 4 || e == 5;
+                    if (off && (ui[e] != 0.0 || dd[e] != 0.0)) diag = false;
+                    if ((e & 1) && (ui[e] != 0.0 || dd[e] != 0.0)) real = false;
+                }
+                mp.kind[b][t] = (int8_t)((diag ? kStageDiag : real ? kStageReal : kStageGeneral) |
+                                         (has_d ? 0 : kStageNoDeriv));
             }
             if (!st.ok()) break;
             mp.nwork = 1ull << (n - M);
-            const uint64_t nb64 = (mp.nwork + 255) / 256;
-            const unsigned nb = (unsigned)std::max<uint64_t>(
-                1, std::min<uint64_t>(nb64, (uint64_t)kReduceBlocks * 4 / kMultiComps));
-#define QI_AM(T, MM, SS) k_adjoint_multi<T, MM, SS><<<nb, 256, 0, s->stream>>>( \
-                (Cx<T>::V2 *)s->amps, (Cx<T>::V2 *)lam->amps, mp, s->d_partials)
+            unsigned nb = 1;
+#define QI_AM(T, MM, SS) st = launch_adjoint_multi<T, MM, SS>(s, lam, mp, &nb)
 #define QI_AM_S(T, MM) { if (S == 1) QI_AM(T, MM, 1); else QI_AM(T, MM, 2); }
             if (f32) {
                 if (M == 1) QI_AM_S(float, 1) else if (M == 2) QI_AM_S(float, 2)
@@ -425,10 +683,11 @@ extern "C" qi_status qi_adjoint_gradient(qi_state *s, const qi_gate *gates, int6
             }
 #undef QI_AM_S
 #undef QI_AM
+            if (!st.ok()) break;
             slot -= M * S;
             k_finalize_to<<<1, 256, 0, s->stream>>>(s->d_partials, (int)nb, M * S, kMultiComps, d_gres + slot);
             count_launch(2);
-            st = check_launch("k_adjoint_multi");
+            st = check_launch("k_finalize_to");
             for (auto &cp : comp_param) slot_param.push_back({slot + cp.first, cp.second});
             j = jj;
             continue;

@@ -15,8 +15,10 @@
 
 #include <algorithm>
 #include <cmath>
+#include <complex>
 #include <map>
 #include <type_traits>
+#include <vector>
 
 namespace qi {
 
@@ -811,6 +813,166 @@ __global__ void __launch_bounds__(256) k_sumop_apply(typename Cx<T>::V2 *o, cons
     }
 }
 
+// FP32 SumOp::apply.  Per element the gathers of all groups are issued four at a time
+// (independent loads in flight), and the largest group's factor — typically the diagonal
+// ZZ / Z terms — comes from byte tables: T_b[v] sums the terms whose Z bits lie in byte b
+// of the index, evaluated at byte value v, so f(i) = sum_b T_b[(i >> 8b) & 255] plus the
+// few terms that straddle bytes.  IDX = uint32_t below 2^32 amplitudes (one POPC per term).
+template <typename IDX> struct ApplyTerm {
+    IDX zmask;
+    float re, im;
+};
+template <typename IDX> struct ApplyHdr {
+    IDX xmask;
+    int32_t first, count;   // direct terms
+};
+constexpr int kApplyTableMin = 6;   // terms in a group before it gets byte tables
+
+template <typename IDX>
+__device__ __forceinline__ float2 apply_factor(const ApplyTerm<IDX> *t, int n, IDX i) {
+    float re = 0.0f, im = 0.0f;
+    for (int k = 0; k < n; ++k) {
+        const int par = (sizeof(IDX) == 4 ? __popc((uint32_t)(i & t[k].zmask)) : __popcll((uint64_t)(i & t[k].zmask))) & 1;
+        const float sgn = par ? -1.0f : 1.0f;
+        re = fmaf(sgn, t[k].re, re);
+        im = fmaf(sgn, t[k].im, im);
+    }
+    return make_float2(re, im);
+}
+
+template <typename IDX>
+__global__ void __launch_bounds__(256) k_sumop_apply_f32(float2 *o, const float2 *in, uint64_t dim,
+                                                         const ApplyHdr<IDX> *hdrs, int ngroups,
+                                                         const ApplyTerm<IDX> *terms, int nterms,
+                                                         const float2 *tables, int ntables) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float2 *stab = reinterpret_cast<float2 *>(smem_raw);                       // [ntables][256], group 0
+    ApplyHdr<IDX> *shdr = reinterpret_cast<ApplyHdr<IDX> *>(stab + ntables * 256);
+    ApplyTerm<IDX> *sterm = reinterpret_cast<ApplyTerm<IDX> *>(shdr + ngroups);
+    for (int k = threadIdx.x; k < ntables * 256; k += blockDim.x) stab[k] = tables[k];
+    for (int k = threadIdx.x; k < ngroups; k += blockDim.x) shdr[k] = hdrs[k];
+    for (int k = threadIdx.x; k < nterms; k += blockDim.x) sterm[k] = terms[k];
+    __syncthreads();
+    using X = Cx<float>;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i64 = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i64 < dim; i64 += stride) {
+        const IDX i = (IDX)i64;
+        float2 acc = make_float2(0.0f, 0.0f);
+        int g0 = 0;
+        if (ntables > 0) {   // group 0: byte tables + straddling terms
+            const float2 v = in[i ^ shdr[0].xmask];
+            float2 f = apply_factor(sterm + shdr[0].first, shdr[0].count, i);
+            for (int b = 0; b < ntables; ++b) {
+                const float2 t = stab[b * 256 + (int)((i >> (8 * b)) & 255)];
+                f.x += t.x;
+                f.y += t.y;
+            }
+            acc = X::fma(f, v, acc);
+            g0 = 1;
+        }
+        for (int g = g0; g < ngroups; g += 4) {
+            float2 v[4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+                if (g + j < ngroups) v[j] = in[i ^ shdr[g + j].xmask];
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+                if (g + j < ngroups) acc = X::fma(apply_factor(sterm + shdr[g + j].first, shdr[g + j].count, i), v[j], acc);
+        }
+        o[i64] = acc;
+    }
+}
+
+// Host side of k_sumop_apply_f32: term records, the byte tables of the largest group (moved
+// to index 0) and the shared-memory size.
+template <typename IDX>
+struct ApplyPlan {
+    std::vector<ApplyHdr<IDX>> hdrs;
+    std::vector<ApplyTerm<IDX>> terms;
+    std::vector<float2> tables;
+    int ntables = 0;
+    size_t smem() const {
+        return tables.size() * sizeof(float2) + hdrs.size() * sizeof(ApplyHdr<IDX>) + terms.size() * sizeof(ApplyTerm<IDX>);
+    }
+};
+
+template <typename IDX>
+static void build_apply_plan(int n, const std::vector<GroupHdr> &hdrs, const std::vector<GroupTerm> &gts,
+                             ApplyPlan<IDX> &ap) {
+    int big = -1;
+    for (size_t g = 0; g < hdrs.size(); ++g)
+        if (hdrs[g].count >= kApplyTableMin && (big < 0 || hdrs[g].count > hdrs[(size_t)big].count)) big = (int)g;
+    std::vector<size_t> order;
+    if (big >= 0) order.push_back((size_t)big);
+    for (size_t g = 0; g < hdrs.size(); ++g)
+        if ((int)g != big) order.push_back(g);
+    const int nbytes = (n + 7) / 8;
+    std::vector<std::complex<double>> tab;
+    for (size_t g : order) {
+        const GroupHdr &h = hdrs[g];
+        ApplyHdr<IDX> ah;
+        ah.xmask = (IDX)h.xmask;
+        ah.first = (int32_t)ap.terms.size();
+        const bool tabled = (int)g == big;
+        if (tabled) tab.assign((size_t)nbytes * 256, std::complex<double>(0, 0));
+        for (int k = 0; k < h.count; ++k) {
+            const GroupTerm &t = gts[(size_t)(h.first + k)];
+            int byte = -1;
+            if (tabled) {
+                if (t.zmask == 0) byte = 0;
+                for (int b = 0; b < nbytes && byte < 0; ++b)
+                    if ((t.zmask & ~(0xffull << (8 * b))) == 0) byte = b;
+            }
+            if (byte >= 0) {
+                const uint64_t zb = (t.zmask >> (8 * byte)) & 0xff;
+                for (int v = 0; v < 256; ++v) {
+                    const double sgn = (__builtin_popcountll((uint64_t)v & zb) & 1) ? -1.0 : 1.0;
+                    tab[(size_t)byte * 256 + (size_t)v] += std::complex<double>(sgn * t.re, sgn * t.im);
+                }
+            } else {
+                ap.terms.push_back(ApplyTerm<IDX>{(IDX)t.zmask, (float)t.re, (float)t.im});
+            }
+        }
+        ah.count = (int32_t)ap.terms.size() - ah.first;
+        ap.hdrs.push_back(ah);
+        if (tabled) {
+            ap.ntables = nbytes;
+            for (auto &c : tab) ap.tables.push_back(make_float2((float)c.real(), (float)c.imag()));
+        }
+    }
+}
+
+template <typename IDX>
+static Status launch_sumop_apply_f32(qi_state *o, qi_state *in, const std::vector<GroupHdr> &hdrs,
+                                     const std::vector<GroupTerm> &gts, bool *done) {
+    ApplyPlan<IDX> ap;
+    build_apply_plan<IDX>(o->n, hdrs, gts, ap);
+    const size_t sm = ap.smem();
+    *done = false;
+    if (sm > 200 * 1024) return ok_status();   // the caller takes the generic kernel
+    ApplyHdr<IDX> *d_hdr = nullptr;
+    ApplyTerm<IDX> *d_term = nullptr;
+    float2 *d_tab = nullptr;
+    QI_CUDA(cudaMallocAsync((void **)&d_hdr, std::max<size_t>(1, ap.hdrs.size()) * sizeof(ApplyHdr<IDX>), o->stream));
+    QI_CUDA(cudaMallocAsync((void **)&d_term, std::max<size_t>(1, ap.terms.size()) * sizeof(ApplyTerm<IDX>), o->stream));
+    QI_CUDA(cudaMallocAsync((void **)&d_tab, std::max<size_t>(1, ap.tables.size()) * sizeof(float2), o->stream));
+    QI_CUDA(cudaMemcpyAsync(d_hdr, ap.hdrs.data(), ap.hdrs.size() * sizeof(ApplyHdr<IDX>), cudaMemcpyHostToDevice, o->stream));
+    QI_CUDA(cudaMemcpyAsync(d_term, ap.terms.data(), ap.terms.size() * sizeof(ApplyTerm<IDX>), cudaMemcpyHostToDevice,
+                            o->stream));
+    QI_CUDA(cudaMemcpyAsync(d_tab, ap.tables.data(), ap.tables.size() * sizeof(float2), cudaMemcpyHostToDevice, o->stream));
+    auto kern = k_sumop_apply_f32<IDX>;
+    if (sm > 48 * 1024) QI_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    kern<<<pgrid(o->dim()), 256, sm, o->stream>>>((float2 *)o->amps, (const float2 *)in->amps, o->dim(), d_hdr,
+                                                 (int)ap.hdrs.size(), d_term, (int)ap.terms.size(), d_tab, ap.ntables);
+    count_launch();
+    Status st = check_launch("k_sumop_apply_f32");
+    QI_CUDA(cudaFreeAsync(d_hdr, o->stream));
+    QI_CUDA(cudaFreeAsync(d_term, o->stream));
+    QI_CUDA(cudaFreeAsync(d_tab, o->stream));
+    *done = st.ok();
+    return st;
+}
+
 // Build the grouped representation of a term list (host).
 static void group_terms(const qi_pauli_term *terms, int64_t nt, std::vector<GroupHdr> &hdrs,
                         std::vector<GroupTerm> &out) {
@@ -977,6 +1139,12 @@ Status sumop_apply(qi_state *o, qi_state *in, const qi_pauli_term *terms, int64_
     std::vector<GroupHdr> hdrs;
     std::vector<GroupTerm> gts;
     group_terms(terms, nt, hdrs, gts);
+    if (o->prec == QI_F32) {
+        bool done = false;
+        Status st = o->n <= 32 ? launch_sumop_apply_f32<uint32_t>(o, in, hdrs, gts, &done)
+                               : launch_sumop_apply_f32<uint64_t>(o, in, hdrs, gts, &done);
+        if (!st.ok() || done) return st;
+    }
     GroupHdr *d_hdr = nullptr;
     GroupTerm *d_terms = nullptr;
     Status st = upload_groups(o, hdrs, gts, &d_hdr, &d_terms);

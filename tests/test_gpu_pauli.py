@@ -55,6 +55,42 @@ def test_sumop_apply_and_expectation(qi, orc, prec):
             assert abs(e - e_want) < (1e-11 if prec == 0 else 2e-5)
 
 
+def diagonal_heavy_terms(n, seed):
+    """Many Z-only terms (so one x-mask group gets byte tables): random Z masks within one
+    byte and across bytes, an identity term, complex coefficients; plus a few X/Y terms."""
+    rng = np.random.default_rng(seed)
+    out = [workloads.term(complex(0.3, -0.2), [])]
+    for _ in range(30):
+        w = int(rng.integers(1, min(4, n) + 1))
+        qs = rng.choice(n, w, replace=False)
+        out.append(workloads.term(complex(rng.uniform(-1, 1), rng.uniform(-0.5, 0.5)), [(int(q), "Z") for q in qs]))
+    for _ in range(8):
+        qs = rng.choice(n, 2, replace=False)
+        out.append(workloads.term(complex(rng.uniform(-1, 1), 0.0), [(int(qs[0]), "X"), (int(qs[1]), "Y")]))
+    return workloads.terms_array(out)
+
+
+@pytest.mark.parametrize("case", ["xxz20", "diag13", "diag18", "lattice16"])
+def test_sumop_apply_f32_tabled_group(qi, orc, case):
+    """FP32 SumOp::apply with the largest x-mask group evaluated from byte tables (ZZ / Z
+    terms, straddling bonds such as (7, 8) and the periodic (0, n-1)) against the oracle."""
+    if case == "xxz20":
+        n, terms = 20, workloads.xxz_periodic(20, seed=3)
+    elif case == "lattice16":
+        n, terms = 16, workloads.lattice_xyz(4, 4, seed=1)
+    else:
+        n = int(case[4:])
+        terms = diagonal_heavy_terms(n, n)
+    init = rand_state(n, 11 + n)
+    want = orc.sumop_apply(init, n, terms)
+    with qi.DeviceState(n, 1) as st, qi.DeviceState(n, 1) as out:
+        st.upload(init)
+        qi.sumop_apply(out, st, terms)
+        got = out.download()
+    scale = float(np.sum(np.abs(terms["re"]) + np.abs(terms["im"])))
+    assert np.max(np.abs(got - want)) < 2e-6 * scale
+
+
 def test_heisenberg_expectation_20q(qi, orc):
     n = 20
     init = rand_state(n, 1)

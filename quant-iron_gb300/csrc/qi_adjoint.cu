@@ -601,6 +601,8 @@ extern "C" qi_status qi_adjoint_gradient(qi_state *s, const qi_gate *gates, int6
         return !m.pauli && m.nt == 1 && m.controls.empty() && n_params(jj) <= 1;
     };
     std::vector<std::unique_ptr<qi_plan>> seg_plans;   // kept until the sweep has run
+    void *const psi_home = s->amps;   // psi's own buffer: holds psi again before returning
+    void *scratch = nullptr;          // third state buffer for affine gathers (rotates with psi, lambda)
     for (int64_t j = n_gates - 1; j >= 0 && st.ok();) {
         // single-qubit gates, consecutive in reverse, on at most kMultiQubits qubits with at
         // most kMultiStages gates each: one pass for the group
@@ -695,6 +697,36 @@ extern "C" qi_status qi_adjoint_gradient(qi_state *s, const qi_gate *gates, int6
         // fixed gates, consecutive in reverse: their inverses as one fused plan on psi and lambda
         for (jj = j; jj >= 0 && n_params(jj) == 0; --jj) {}
         if (j - jj >= 2 && plan_opts.fusion != QI_FUSION_NONE) {
+            // only X / CNOT / SWAP: one index permutation per state, out[x] = in[f(x)] with f
+            // the run's forward map (gathering through f un-applies the run)
+            int moves = 0;
+            bool affine = true;
+            for (int64_t k = j; k > jj; --k) {
+                if (mats[(size_t)k].nt == 0) continue;
+                affine = affine && affine_gate(mats[(size_t)k]);
+                ++moves;
+            }
+            if (affine && moves >= 2) {
+                AffineMap am;
+                affine_identity(am);
+                for (int64_t k = jj + 1; k <= j; ++k)
+                    if (mats[(size_t)k].nt != 0) affine_compose(am, mats[(size_t)k]);
+                if (!scratch) {
+                    e = cudaMalloc(&scratch, s->bytes());
+                    if (e != cudaSuccess) {
+                        scratch = nullptr;
+                        st = cuda_status(e, "cudaMalloc(permutation buffer)");
+                        break;
+                    }
+                }
+                for (qi_state *q : {s, lam}) {
+                    st = affine_gather_async(s, scratch, q->amps, am);
+                    if (!st.ok()) break;
+                    std::swap(q->amps, scratch);
+                }
+                j = jj;
+                continue;
+            }
             std::vector<Elem> inv;
             for (int64_t k = j; k > jj; --k) {
                 GateMatrix gi = mats[(size_t)k];
@@ -787,6 +819,15 @@ extern "C" qi_status qi_adjoint_gradient(qi_state *s, const qi_gate *gates, int6
         for (auto &sp : slot_param) grads_out[sp.second] += 2.0 * h[(size_t)sp.first];
     }
     cudaStreamSynchronize(s->stream);
+    if (s->amps != psi_home) {   // psi_home is lambda's or the scratch buffer now
+        e = cudaMemcpyAsync(psi_home, s->amps, s->bytes(), cudaMemcpyDeviceToDevice, s->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+        if (e != cudaSuccess && st.ok()) st = cuda_status(e, "restore psi buffer");
+        if (lam->amps == psi_home) lam->amps = s->amps;
+        else scratch = s->amps;
+        s->amps = psi_home;
+    }
+    if (scratch) cudaFree(scratch);
     for (auto &sp : seg_plans) {
         if (sp->d_mats) cudaFree(sp->d_mats);
         if (sp->d_tc) cudaFree(sp->d_tc);

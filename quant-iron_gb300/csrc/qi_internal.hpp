@@ -137,6 +137,19 @@ struct GateMatrix {
     double alpha_re = 0, alpha_im = 0;
 };
 
+// GF(2)-affine index map of a run of X / CNOT / SWAP gates (qi_permute.cu):
+// bit k of f(j) = parity(row[k] & j) ^ bit k of b.
+constexpr int kAffineMaxBytes = 5;   // index bytes (states up to 40 qubits)
+struct AffineMap {
+    uint64_t row[64];
+    uint64_t b;
+};
+bool affine_gate(const GateMatrix &gm);   // X / CNOT with at most one control, or uncontrolled SWAP
+void affine_identity(AffineMap &m);
+void affine_compose(AffineMap &m, const GateMatrix &gm);   // m := gate o m
+// out[j] = in[f(j)] for every amplitude j of s's size and precision (out != in), on s's stream.
+Status affine_gather_async(qi_state *s, void *out, const void *in, const AffineMap &m);
+
 Status validate_gate(int n, const qi_gate &g);
 // Validate + build the matrix of a (resolved) gate.
 Status gate_to_matrix(int n, const qi_gate &g, GateMatrix *out);

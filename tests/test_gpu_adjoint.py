@@ -183,3 +183,46 @@ def test_grouped_reverse_sweep_vs_per_gate_and_fd(qi, orc, n):
     ids = sorted(int(x) for x in rng.choice(theta.size, min(12, theta.size), replace=False))
     g_ref = fd_grad(orc, n, gates, theta, terms, init, ids)
     assert np.linalg.norm(g64[ids] - g_ref) / np.linalg.norm(g_ref) < 1e-6
+
+
+@pytest.mark.parametrize("layers", [1, 2, 3])
+@pytest.mark.parametrize("prec", [0, 1], ids=["f64", "f32"])
+def test_permutation_runs_in_reverse_sweep(qi, orc, layers, prec):
+    """Runs of X / CNOT / SWAP / singly-controlled X between rotation layers are un-applied
+    as one index permutation per state (psi and lambda move between three buffers; an odd
+    number of runs leaves psi in another buffer, which the call copies back): gradients
+    equal the per-gate sweep and the state returns to the initial one."""
+    n = 11
+    rng = np.random.default_rng(layers)
+    gl = workloads.GateList()
+    npar = 0
+    for _ in range(layers):
+        for q in range(n):
+            gl.add("RY", [q], [], [0.0], [npar])
+            gl.add("RZ", [q], [], [0.0], [npar + 1])
+            npar += 2
+        for q in range(n - 1):
+            gl.add("CNOT", [q + 1], [q])
+        gl.add("SWAP", [0, n - 1])
+        gl.add("X", [3])
+        gl.add("X", [5], [2])
+        gl.add("CNOT", [0], [n - 1])
+    theta = rng.uniform(-np.pi, np.pi, size=npar)
+    terms = workloads.xxz_periodic(n, seed=4)
+    init = workloads.plus_state(n)
+    res = {}
+    for fusion in (qi.FUSION_NONE, qi.FUSION_GREEDY):
+        with qi.DeviceState(n, prec) as st:
+            st.upload(init)
+            e, g = qi.adjoint_gradient(st, gates=gl.array(), theta=theta, terms=terms, fusion=fusion)
+            back = st.download()
+        assert np.max(np.abs(back - init)) < (1e-12 if prec == 0 else 1e-5)
+        res[fusion] = (e, g)
+    (e0, g0), (e1, g1) = res[qi.FUSION_NONE], res[qi.FUSION_GREEDY]
+    assert np.linalg.norm(g1 - g0) / np.linalg.norm(g0) < (1e-10 if prec == 0 else 1e-4)
+    if prec == 0:
+        e_ref = energy_oracle(orc, n, gl.array(), theta, terms, init)
+        assert abs(e1 - e_ref) < 1e-12
+        ids = list(range(0, npar, 7))
+        g_ref = fd_grad(orc, n, gl.array(), theta, terms, init, ids)
+        assert np.linalg.norm(g1[ids] - g_ref) / np.linalg.norm(g_ref) < 1e-6

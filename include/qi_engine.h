@@ -379,9 +379,10 @@ typedef struct qi_plan_op_info {
     int32_t  kind;          /* 1 one-target gate, 2 SWAP, 3 two-target gate, 4 fused dense block,
                                5 Pauli exponential, 6 Pauli string + normalise, 7 diagonal block,
                                8 renormalisation, 9 phase polynomial (a run of diagonal blocks),
-                               10 grouped Pauli exponentials (a run with X-masks in {0, X}) */
+                               10 grouped Pauli exponentials (a run with X-masks in {0, X}),
+                               11 qubit permutation (a run of SWAP / X gates; qi_plan_op_bitperm) */
     int32_t  k;             /* number of targets (kind 9: number of diagonal blocks in the run;
-                               kind 10: number of exponentials in the run) */
+                               kind 10: number of exponentials in the run; kind 11: gates in the run) */
     int32_t  targets[6];    /* sorted ascending for kinds 3, 4, 7 */
     int32_t  tensor_cores;  /* kind 4: 1 if the block runs on the tcgen05 tensor-core kernel */
     int32_t  phase_poly;    /* kind 4: 1 if a phase polynomial (qi_plan_op_phase_poly) follows the block
@@ -394,6 +395,11 @@ typedef struct qi_plan_op_info {
                                kind 10: the tables (see qi_plan_op_pauli_group), else 0 */
 } qi_plan_op_info;
 qi_status qi_plan_num_ops(const qi_plan *p, int64_t *out);
+/* Kind 11 ops: the state after the op is out[j] = in[s(j)] with
+ * s(j) = flip ^ sum_k ((j >> k) & 1) << source_bit[k]  (source_bit: num_qubits entries).
+ * No reference counterpart: the reference applies each SWAP / X on its own
+ * (operator.rs SWAP and Pauli-X apply). */
+qi_status qi_plan_op_bitperm(const qi_plan *p, int64_t i, int32_t *source_bit, uint64_t *flip);
 qi_status qi_plan_op_get(const qi_plan *p, int64_t i, qi_plan_op_info *info, double *matrix_out, int64_t capacity);
 /* Kind 9 ops, and kind 4 ops with phase_poly = 1 (applied after the block): the phase
  * polynomial f(x) = c0 + sum_q a[q] x_q + sum_{q<r} b[q*n+r] x_q x_r applied as

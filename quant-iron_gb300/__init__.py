@@ -249,6 +249,13 @@ class Plan:
                     tables.append((basis[8 * t:8 * t + rank[t]].copy(), tab.reshape(-1, 2, 2) if per == 4 else tab))
                     off += cnt
                 op["group"] = tables
+            if info.kind == 11:   # qubit permutation: out[j] = in[flip ^ sum_k bit_k(j) << source_bit[k]]
+                src = np.zeros(self.num_qubits, dtype=np.int32)
+                flip = ctypes.c_uint64()
+                check(lib.qi_plan_op_bitperm(self.h, i, src.ctypes.data, ctypes.byref(flip)))
+                op["source_bit"] = src
+                op["flip"] = int(flip.value)
+                op["targets"] = []
             out.append(op)
         return out
 
@@ -339,7 +346,7 @@ def trotter_evolve(state, terms, dt, num_steps, order=1, observable=None, observ
 
 KERNEL_OF_OP_KIND = {1: "k_mat1", 2: "k_swap", 3: "k_mat2", 4: "k_fused", 5: "k_pauli_exp", 6: "k_pauli_exp+normalise",
                      7: "k_diagk", 8: "k_norm_partial+k_normalise_apply", 9: "k_phase_poly",
-                     10: "k_pauli_group_diag|k_pauli_group_pair"}
+                     10: "k_pauli_group_diag|k_pauli_group_pair", 11: "k_bitperm"}
 
 
 def plan_profile(plan, state):

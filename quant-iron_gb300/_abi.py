@@ -205,5 +205,7 @@ lib.qi_plan_op_phase_poly.restype = _i32
 lib.qi_plan_op_phase_poly.argtypes = [_vp, _i64, ctypes.POINTER(_u64), _vp, _vp]
 lib.qi_plan_op_pauli_group.restype = _i32
 lib.qi_plan_op_pauli_group.argtypes = [_vp, _i64, ctypes.POINTER(_i32), _vp, _vp]
+lib.qi_plan_op_bitperm.restype = _i32
+lib.qi_plan_op_bitperm.argtypes = [_vp, _i64, _vp, ctypes.POINTER(ctypes.c_uint64)]
 lib.qi_adjoint_gradient.restype = _i32
 lib.qi_adjoint_gradient.argtypes = [_vp, _vp, _i64, _pd, _i64, _vp, _i64, ctypes.POINTER(ExecOptions), _pd, _pd]

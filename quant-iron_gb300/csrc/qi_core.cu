@@ -229,6 +229,32 @@ __global__ void k_normalise_apply(typename Cx<T>::V2 *a, uint64_t dim, const dou
     }
 }
 
+// out = in / norm for a permuted copy moving back to the state's own buffer: always writes
+// (a norm of 0 or 1 copies unchanged; 0 also flags ZeroNorm).
+template <typename T>
+__global__ void k_normalise_to(typename Cx<T>::V2 *__restrict__ out, const typename Cx<T>::V2 *__restrict__ in,
+                               uint64_t dim, const double *result, int *flag) {
+    __shared__ T s_inv;
+    if (threadIdx.x == 0) {
+        const double norm = sqrt(result[0]);
+        if (norm == 0.0 && blockIdx.x == 0) *flag = 1;
+        s_inv = (T)(norm != 0.0 && norm != 1.0 ? 1.0 / norm : 1.0);
+    }
+    __syncthreads();
+    const T inv = s_inv;
+    constexpr int U = 4;
+    const uint64_t step = blockDim.x, stride = (uint64_t)gridDim.x * blockDim.x * U;
+    for (uint64_t base = blockIdx.x * (uint64_t)blockDim.x * U + threadIdx.x; base < dim; base += stride) {
+        typename Cx<T>::V2 v[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+            if (base + u * step < dim) v[u] = in[base + u * step];
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+            if (base + u * step < dim) out[base + u * step] = Cx<T>::make(v[u].x * inv, v[u].y * inv);
+    }
+}
+
 // ---------------------------------------------------------------- helpers --
 static unsigned grid_for(uint64_t work, unsigned threads = 256, unsigned cap = 152 * 16) {
     uint64_t g = (work + threads - 1) / threads;
@@ -324,6 +350,38 @@ Status state_normalise_device_async(qi_state *s) {
         k_normalise_apply<double><<<g, 256, 0, s->stream>>>((double2 *)s->amps, s->dim(), s->d_result, s->d_flag);
     count_launch();
     return check_launch("k_normalise_apply");
+}
+
+Status state_normalise_device_to_async(qi_state *s, void *out, const void *in) {
+    unsigned nb;
+    void *const home = s->amps;
+    s->amps = const_cast<void *>(in);   // the norm of `in`
+    Status st = norm_async(s, &nb);
+    s->amps = home;
+    if (!st.ok()) return st;
+    k_finalize<<<1, 256, 0, s->stream>>>(s->d_partials, (int)nb, 1, s->d_result);
+    count_launch();
+    unsigned g = grid_for(s->dim());
+    if (s->prec == QI_F32)
+        k_normalise_to<float><<<g, 256, 0, s->stream>>>((float2 *)out, (const float2 *)in, s->dim(), s->d_result, s->d_flag);
+    else
+        k_normalise_to<double><<<g, 256, 0, s->stream>>>((double2 *)out, (const double2 *)in, s->dim(), s->d_result,
+                                                         s->d_flag);
+    count_launch();
+    return check_launch("k_normalise_to");
+}
+
+Status state_scratch(qi_state *s, void **out) {
+    if (!s->d_scratch) {
+        cudaError_t e = cudaMalloc(&s->d_scratch, s->bytes());
+        if (e != cudaSuccess) {
+            s->d_scratch = nullptr;
+            cudaGetLastError();   // clear the allocation error: the caller falls back
+            return cuda_status(e, "cudaMalloc(second state buffer)");
+        }
+    }
+    *out = s->d_scratch;
+    return ok_status();
 }
 
 Status state_read_flag(qi_state *s, int *flag) {
@@ -440,6 +498,7 @@ qi_status qi_state_destroy(qi_state *s) {
         if (s->h_result) cudaFreeHost(s->h_result);
         if (s->d_flag) cudaFree(s->d_flag);
         if (s->d_staging) cudaFree(s->d_staging);
+        if (s->d_scratch) cudaFree(s->d_scratch);
         if (s->own_stream) cudaStreamDestroy(s->own_stream);
     }
     delete s;

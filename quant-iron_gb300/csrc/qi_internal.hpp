@@ -64,6 +64,7 @@ struct qi_state {
     void *d_staging = nullptr;        // host<->device conversion staging (lazy)
     size_t staging_bytes = 0;
     int *d_flag = nullptr;            // device-side error flag (ZeroNorm inside async sequences)
+    void *d_scratch = nullptr;        // second state buffer for out-of-place permutations (lazy)
 
     uint64_t dim() const { return 1ull << n; }
     size_t amp_bytes() const { return prec == QI_F64 ? 16 : 8; }
@@ -94,6 +95,7 @@ enum OpKind : int32_t {
     OP_NORMALISE = 8,     // FP64 norm on the device, divide (periodic renormalisation)
     OP_PHASE_POLY = 9,    // run of diagonal blocks as one quadratic phase polynomial over all qubits (FP32)
     OP_PAULI_GROUP = 10,  // run of Pauli exponentials with X-masks in {0, X}: parity-indexed table, one pass
+    OP_BITPERM = 11,      // run of SWAP / X gates as one qubit permutation: out[j] = in[s(j)] (tiled transpose)
 };
 // OP_PAULI_GROUP limits: diagonal runs use up to kGroupChunks tables of up to
 // 2^kGroupRank factors; pair runs one table of up to 2^kPairRank 2x2 matrices.
@@ -120,6 +122,8 @@ struct Op {
     int32_t nchunk = 0;
     int32_t rank[kGroupChunks] = {0, 0, 0, 0};
     uint64_t basis[kGroupChunks * kGroupRank] = {0};
+    // OP_BITPERM: s(j) = xmask ^ sum_k bit k of j << perm[k] (the source of output index j)
+    int8_t perm[64] = {0};
 };
 
 // Host-side description of a gate after validation: 2x2 / 4x4 matrix on its
@@ -149,6 +153,16 @@ void affine_identity(AffineMap &m);
 void affine_compose(AffineMap &m, const GateMatrix &gm);   // m := gate o m
 // out[j] = in[f(j)] for every amplitude j of s's size and precision (out != in), on s's stream.
 Status affine_gather_async(qi_state *s, void *out, const void *in, const AffineMap &m);
+// Qubit permutation (tiled through shared memory, coalesced on both sides):
+// out[j] = in[flip ^ sum_k bit k of j << perm[k]], out != in.
+Status bitperm_async(qi_state *s, void *out, const void *in, const int8_t *perm, uint64_t flip);
+// The same permutation in place, as one SWAP per transposition of perm's cycles and one X per
+// flipped bit (used when no second state buffer can be allocated).
+Status bitperm_in_place_async(qi_state *s, const int8_t *perm, uint64_t flip);
+// The state's second buffer (allocated on first use, freed with the state).
+Status state_scratch(qi_state *s, void **out);
+// Divide in by its FP64 norm into out (out != in; a norm of 0 or 1 copies unchanged, 0 flags ZeroNorm).
+Status state_normalise_device_to_async(qi_state *s, void *out, const void *in);
 
 Status validate_gate(int n, const qi_gate &g);
 // Validate + build the matrix of a (resolved) gate.

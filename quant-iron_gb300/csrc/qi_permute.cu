@@ -10,6 +10,7 @@
 #include "qi_device.cuh"
 
 #include <algorithm>
+#include <cstring>
 #include <utility>
 
 namespace qi {
@@ -112,6 +113,160 @@ Status affine_gather_async(qi_state *s, void *out, const void *in, const AffineM
     }
     count_launch();
     return check_launch("k_affine_gather");
+}
+
+// ---------------------------------------------------------------- qubit permutations
+// out[j] = in[s(j)], s(j) = flip ^ sum_k bit k of j << perm[k].  A tile is every index that
+// varies only in the tile bits T = {0..4} (output side) and {k : perm[k] <= 4} (their
+// sources' lowest bits), so both the reads (consecutive source bits 0..4) and the writes
+// (consecutive output bits 0..4) run over 32 consecutive amplitudes; the tile passes
+// through shared memory (one pad slot per 32 entries against bank conflicts).
+constexpr int kPermTileBits = 10;
+struct BitPermParams {
+    uint64_t flip;
+    uint64_t ntiles;
+    int32_t nt, no;                  // tile bits, outer bits
+    int8_t tbits[kPermTileBits];     // tile bits (output side), ascending
+    int8_t sbits[kPermTileBits];     // their sources, ascending
+    int8_t sdst[kPermTileBits];      // source tile bit i comes from tile bit sdst[i]
+    int8_t obits[64];                // outer bits (output side), ascending
+    int8_t perm[64];
+};
+
+__device__ __forceinline__ uint32_t pad32(uint32_t e) { return e + (e >> 5); }
+
+template <typename V2>
+__global__ void __launch_bounds__(256) k_bitperm(V2 *__restrict__ out, const V2 *__restrict__ in,
+                                                 const __grid_constant__ BitPermParams p) {
+    __shared__ V2 tile[(1 << kPermTileBits) + (1 << kPermTileBits) / 32];
+    __shared__ uint64_t rd_off[1 << kPermTileBits], wr_off[1 << kPermTileBits];
+    __shared__ uint16_t rd_dst[1 << kPermTileBits];
+    __shared__ uint64_t dep_j[2 * kAffineMaxBytes][16], dep_s[2 * kAffineMaxBytes][16];   // per 4-bit nibble
+    const int te = 1 << p.nt;
+    for (int e = threadIdx.x; e < te; e += blockDim.x) {
+        uint64_t ro = 0, wo = 0;
+        uint32_t dst = 0;
+        for (int i = 0; i < p.nt; ++i)
+            if ((e >> i) & 1) {
+                ro |= 1ull << p.sbits[i];
+                wo |= 1ull << p.tbits[i];
+                dst |= 1u << p.sdst[i];
+            }
+        rd_off[e] = ro;
+        wr_off[e] = wo;
+        rd_dst[e] = (uint16_t)pad32(dst);
+    }
+    // outer index t -> (output base, source base) by one table lookup per nibble of t
+    const int nnib = (p.no + 3) / 4;
+    for (int k = threadIdx.x; k < nnib * 16; k += blockDim.x) {
+        const int b = k >> 4, v = k & 15;
+        uint64_t dj = 0, ds = 0;
+        for (int e = 0; e < 4; ++e) {
+            const int i = 4 * b + e;
+            if (i < p.no && ((v >> e) & 1)) {
+                dj |= 1ull << p.obits[i];
+                ds |= 1ull << p.perm[p.obits[i]];
+            }
+        }
+        dep_j[b][v] = dj;
+        dep_s[b][v] = ds;
+    }
+    __syncthreads();
+    for (uint64_t t = blockIdx.x; t < p.ntiles; t += gridDim.x) {
+        uint64_t bj = 0, bs = p.flip;
+        for (int b = 0; b < nnib; ++b) {
+            const int v = (int)((t >> (4 * b)) & 15);
+            bj |= dep_j[b][v];
+            bs ^= dep_s[b][v];
+        }
+        for (int e = threadIdx.x; e < te; e += blockDim.x) tile[rd_dst[e]] = in[bs ^ rd_off[e]];
+        __syncthreads();
+        for (int e = threadIdx.x; e < te; e += blockDim.x) out[bj | wr_off[e]] = tile[pad32((uint32_t)e)];
+        __syncthreads();
+    }
+}
+
+Status bitperm_async(qi_state *s, void *out, const void *in, const int8_t *perm, uint64_t flip) {
+    const int n = s->n;
+    if (n > 8 * kAffineMaxBytes) return err(QI_ERR_UNSUPPORTED, n, 8 * kAffineMaxBytes, "qubit permutation width");
+    BitPermParams p;
+    std::memset(&p, 0, sizeof(p));
+    int src_of[64];   // source bit -> output bit
+    for (int k = 0; k < n; ++k) {
+        p.perm[k] = perm[k];
+        src_of[perm[k]] = k;
+    }
+    bool in_tile[64] = {false};
+    for (int k = 0; k < n; ++k)
+        if (k <= 4 || perm[k] <= 4) in_tile[k] = true;
+    int tpos[64];
+    for (int k = 0; k < n; ++k)
+        if (in_tile[k]) {
+            tpos[k] = p.nt;
+            p.tbits[p.nt++] = (int8_t)k;
+        } else {
+            p.obits[p.no++] = (int8_t)k;
+        }
+    // sources of the tile bits, ascending, each with its tile bit
+    int ns = 0;
+    for (int q = 0; q < n; ++q)
+        if (in_tile[src_of[q]]) {
+            p.sbits[ns] = (int8_t)q;
+            p.sdst[ns] = (int8_t)tpos[src_of[q]];
+            ++ns;
+        }
+    p.flip = flip;
+    p.ntiles = 1ull << p.no;
+    const uint64_t g = std::max<uint64_t>(1, std::min<uint64_t>(p.ntiles, 152 * 4));
+    if (s->prec == QI_F32) k_bitperm<float2><<<(unsigned)g, 256, 0, s->stream>>>((float2 *)out, (const float2 *)in, p);
+    else k_bitperm<double2><<<(unsigned)g, 256, 0, s->stream>>>((double2 *)out, (const double2 *)in, p);
+    count_launch();
+    return check_launch("k_bitperm");
+}
+
+Status bitperm_in_place_async(qi_state *s, const int8_t *perm, uint64_t flip) {
+    // out[j] = in[s(j)] moves the amplitude at source bit perm[k] to output bit k.  Realise the
+    // bit permutation by transpositions: walk output positions k = 0.., swapping the qubit that
+    // currently sits where bit k's source is into place.  cur[q] = the source bit held at q.
+    const int n = s->n;
+    int cur[64], where[64];
+    for (int q = 0; q < n; ++q) cur[q] = where[q] = q;
+    // flips act on the source index: apply them first (X on source bit q)
+    for (int q = 0; q < n; ++q)
+        if ((flip >> q) & 1ull) {
+            qi_gate g;
+            std::memset(&g, 0, sizeof(g));
+            g.kind = QI_GATE_X;
+            g.n_targets = 1;
+            g.targets[0] = q;
+            for (int k = 0; k < 3; ++k) g.param_ids[k] = -1;
+            GateMatrix gm;
+            Status st = gate_to_matrix(n, g, &gm);
+            if (st.ok()) st = launch_op(s, lower_gate(n, gm), nullptr);
+            if (!st.ok()) return st;
+        }
+    for (int k = 0; k < n; ++k) {
+        const int want = perm[k];            // source bit that must end at position k
+        const int at = where[want];
+        if (at == k) continue;
+        qi_gate g;
+        std::memset(&g, 0, sizeof(g));
+        g.kind = QI_GATE_SWAP;
+        g.n_targets = 2;
+        g.targets[0] = k;
+        g.targets[1] = at;
+        for (int j = 0; j < 3; ++j) g.param_ids[j] = -1;
+        GateMatrix gm;
+        Status st = gate_to_matrix(n, g, &gm);
+        if (st.ok()) st = launch_op(s, lower_gate(n, gm), nullptr);
+        if (!st.ok()) return st;
+        const int other = cur[k];
+        cur[k] = want;
+        cur[at] = other;
+        where[want] = k;
+        where[other] = at;
+    }
+    return ok_status();
 }
 
 }  // namespace qi

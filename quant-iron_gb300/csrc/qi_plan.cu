@@ -261,6 +261,72 @@ void compose_block(const std::vector<Elem> &elems, const Block &b, std::vector<i
 }
 
 // ------------------------------------------------------------------ plan ---
+// Runs of at least kPermMinSwaps uncontrolled SWAPs (X gates may sit between them) whose
+// qubits do not fit one fused block: one qubit permutation (a tiled transpose, one pass)
+// instead of the blocks a partition would spend on pure data movement (the SWAP network
+// at the end of a QFT on n qubits fills n / 6 blocks).
+constexpr int kPermMinSwaps = 3;
+
+static bool perm_elem(const Elem &e) {
+    const GateMatrix &g = e.gm;
+    if (e.pauli || !g.controls.empty()) return false;
+    return g.kind == QI_GATE_SWAP || (g.kind == QI_GATE_X && g.nt == 1);
+}
+
+static std::vector<Block> partition_with_permutations(qi_plan *p, const std::vector<Elem> &elems, int kmax) {
+    std::vector<Block> out;
+    size_t seg = 0;   // first element not yet partitioned
+    auto take_segment = [&](size_t end) {
+        if (end <= seg) return;
+        std::vector<Elem> sub(elems.begin() + (long)seg, elems.begin() + (long)end);
+        std::vector<Block> bs = choose_partition(p, sub, kmax);
+        for (Block &b : bs) {
+            for (int &m : b.members) m += (int)seg;
+            out.push_back(std::move(b));
+        }
+    };
+    for (size_t i = 0; i < elems.size();) {
+        if (!perm_elem(elems[i])) {
+            ++i;
+            continue;
+        }
+        size_t j = i;
+        int swaps = 0;
+        uint64_t support = 0;
+        for (; j < elems.size() && perm_elem(elems[j]); ++j) {
+            swaps += elems[j].gm.kind == QI_GATE_SWAP;
+            support |= elems[j].mask;
+        }
+        if (swaps >= kPermMinSwaps && __builtin_popcountll(support) > kmax) {
+            take_segment(i);
+            Block b;
+            b.perm = true;
+            b.mask = support;
+            for (size_t k = i; k < j; ++k) b.members.push_back((int)k);
+            out.push_back(std::move(b));
+            seg = j;
+        }
+        i = j;
+    }
+    take_segment(elems.size());
+    return out;
+}
+
+// The run's gather: applying gates G_1..G_m is out[j] = in[s(j)] with s the inverse of their
+// index map, i.e. the gates' own (self-inverse) maps composed in reverse order.
+static Op bitperm_op(const std::vector<Elem> &elems, const Block &b) {
+    AffineMap g;
+    affine_identity(g);
+    for (auto it = b.members.rbegin(); it != b.members.rend(); ++it) affine_compose(g, elems[(size_t)*it].gm);
+    Op op;
+    op.kind = OP_BITPERM;
+    op.k = (int32_t)b.members.size();
+    op.xmask = g.b;
+    for (int m = 0; m < 64; ++m)   // row m of g is the single bit j_k: source bit m <- output bit k
+        if (g.row[m]) op.perm[__builtin_ctzll(g.row[m])] = (int8_t)m;
+    return op;
+}
+
 Status build_plan(qi_plan *p, std::vector<Elem> &elems) {
     const int n = p->n;
     int fusion = p->opts.fusion;
@@ -332,7 +398,7 @@ Status build_plan(qi_plan *p, std::vector<Elem> &elems) {
             i = j;
         }
     } else {
-        std::vector<Block> blocks = p->partition_override.empty() ? choose_partition(p, elems, kmax)
+        std::vector<Block> blocks = p->partition_override.empty() ? partition_with_permutations(p, elems, kmax)
                                                                   : p->partition_override;
         // compose block matrices in parallel (independent)
         std::vector<std::vector<int>> qb(blocks.size());
@@ -342,7 +408,7 @@ Status build_plan(qi_plan *p, std::vector<Elem> &elems) {
         for (unsigned w = 0; w < nth; ++w) {
             th.emplace_back([&, w] {
                 for (size_t bi = w; bi < blocks.size(); bi += nth)
-                    if (!blocks[bi].single) compose_block(elems, blocks[bi], qb[bi], mb[bi]);
+                    if (!blocks[bi].single && !blocks[bi].perm) compose_block(elems, blocks[bi], qb[bi], mb[bi]);
             });
         }
         for (auto &t : th) t.join();
@@ -385,6 +451,12 @@ Status build_plan(qi_plan *p, std::vector<Elem> &elems) {
             if (b.single) {
                 flush();
                 lower_single(elems[b.members[0]]);
+                continue;
+            }
+            if (b.perm) {
+                flush();
+                p->ops.push_back(bitperm_op(elems, b));
+                p->stats.n_blocks_by_k[0]++;
                 continue;
             }
             bool diag = true;
@@ -489,6 +561,43 @@ Status plan_elems_from_gates(int n, const qi_gate *gates, int64_t ng, const doub
     return ok_status();
 }
 
+// Launches a plan's ops on a state.  OP_BITPERM writes out of place: the amplitudes move to
+// the state's second buffer and back (the next renormalisation writes into the state's own
+// buffer; otherwise one copy at the end), so the state's device pointer never changes.
+struct PlanRunner {
+    qi_plan *p;
+    qi_state *s;
+    void *home;
+    PlanRunner(qi_plan *p_, qi_state *s_) : p(p_), s(s_), home(s_->amps) {}
+    Status op(const Op &o) {
+        if (o.kind == OP_BITPERM) {
+            void *scratch = nullptr;
+            if (s->amps == home && !state_scratch(s, &scratch).ok())
+                return bitperm_in_place_async(s, o.perm, o.xmask);   // no room for a second buffer
+            void *dst = s->amps == home ? scratch : home;
+            Status st = bitperm_async(s, dst, s->amps, o.perm, o.xmask);
+            if (st.ok()) s->amps = dst;
+            return st;
+        }
+        if (o.kind == OP_NORMALISE && s->amps != home) {
+            Status st = state_normalise_device_to_async(s, home, s->amps);
+            if (st.ok()) s->amps = home;
+            return st;
+        }
+        return launch_op(s, o, p->d_mats, p->d_tc);
+    }
+    Status finish(Status st) {   // the amplitudes back in the state's own buffer
+        if (s->amps != home) {
+            if (st.ok()) {
+                cudaError_t e = cudaMemcpyAsync(home, s->amps, s->bytes(), cudaMemcpyDeviceToDevice, s->stream);
+                if (e != cudaSuccess) st = cuda_status(e, "copy back after qubit permutation");
+            }
+            s->amps = home;
+        }
+        return st;
+    }
+};
+
 Status plan_execute(qi_plan *p, qi_state *s) {
     if (s->n != p->n) return err(QI_ERR_INVALID_NUMBER_OF_QUBITS, s->n);   // circuit.rs:161-163
     if (s->prec != p->prec) return err(QI_ERR_UNSUPPORTED, -1, -1, "plan precision differs from state");
@@ -497,10 +606,15 @@ Status plan_execute(qi_plan *p, qi_state *s) {
         if (!up.ok()) return up;
     }
     bool has_norm = false;
+    PlanRunner run(p, s);
     for (const Op &op : p->ops) {
-        Status st = launch_op(s, op, p->d_mats, p->d_tc);
-        if (!st.ok()) return st;
+        Status st = run.op(op);
+        if (!st.ok()) return run.finish(st);
         has_norm = has_norm || op.kind == OP_PAULI_NORM;
+    }
+    {
+        Status st = run.finish(ok_status());
+        if (!st.ok()) return st;
     }
     if (has_norm) {
         int flag = 0;
@@ -579,11 +693,13 @@ qi_status qi_plan_profile(qi_plan *p, qi_state *s, float *ms_out) {
         if (e != cudaSuccess) return publish(cuda_status(e, "cudaEventCreate"));
     }
     Status st = ok_status();
+    PlanRunner run(p, s);
     cudaEventRecord(ev[0], s->stream);
     for (size_t i = 0; i < nops && st.ok(); ++i) {
-        st = launch_op(s, p->ops[i], p->d_mats, p->d_tc);
+        st = run.op(p->ops[i]);
         cudaEventRecord(ev[i + 1], s->stream);
     }
+    st = run.finish(st);
     e = cudaStreamSynchronize(s->stream);
     if (st.ok() && e != cudaSuccess) st = cuda_status(e, "profile");
     for (size_t i = 0; i < nops && st.ok(); ++i) {
@@ -685,6 +801,16 @@ qi_status qi_plan_op_pauli_group(const qi_plan *p, int64_t i, int32_t *n_tables,
     *n_tables = op.nchunk;
     std::copy(op.rank, op.rank + kGroupChunks, rank);
     std::copy(op.basis, op.basis + kGroupChunks * kGroupRank, basis);
+    return publish(ok_status());
+}
+
+qi_status qi_plan_op_bitperm(const qi_plan *p, int64_t i, int32_t *source_bit, uint64_t *flip) {
+    if (!p || !source_bit || !flip) return publish(err(QI_ERR_NULL_ARGUMENT));
+    if (i < 0 || i >= (int64_t)p->ops.size()) return publish(err(QI_ERR_INVALID_INPUT_VALUE, i));
+    const Op &op = p->ops[(size_t)i];
+    if (op.kind != OP_BITPERM) return publish(err(QI_ERR_INVALID_INPUT_VALUE, op.kind, OP_BITPERM));
+    for (int k = 0; k < p->n; ++k) source_bit[k] = op.perm[k];
+    *flip = op.xmask;
     return publish(ok_status());
 }
 

@@ -22,6 +22,7 @@ struct Block {
     std::vector<int> members;   // element indices, in application order
     uint64_t mask = 0;          // qubits of the block
     bool single = false;        // lowered as one per-gate op
+    bool perm = false;          // a run of SWAP / X gates lowered as one qubit permutation
 };
 
 std::vector<Block> greedy_partition(const std::vector<Elem> &elems, int n, int kmax);

@@ -78,6 +78,12 @@ def replay(ops, n, init):
             s = ch * s + sh * ph * s[idx ^ x]
         elif kind == 10:
             s = _replay_pauli_group(s, n, op)
+        elif kind == 11:   # qubit permutation: out[j] = in[flip ^ sum_k bit_k(j) << source_bit[k]]
+            idx = np.arange(1 << n, dtype=np.int64)
+            src = np.full(1 << n, op["flip"], dtype=np.int64)
+            for k in range(n):
+                src ^= ((idx >> k) & 1) << int(op["source_bit"][k])
+            s = s[src]
         else:
             raise AssertionError("unexpected op kind %d" % kind)
     return s
@@ -120,7 +126,7 @@ def test_greedy_fusion_replay_matches_oracle(qi, orc, kmax, seed):
     want = orc.execute(init, n, gates)
     plan = qi.Plan(n, qi.F64, gates, fusion=qi.FUSION_GREEDY, max_block_qubits=kmax)
     ops = plan.ops()
-    assert all(op["k"] <= kmax for op in ops)
+    assert all(op["k"] <= kmax for op in ops if op["kind"] != 11)
     got = replay(ops, n, init)
     assert np.max(np.abs(got - want)) < 1e-12
     st = plan.stats()
@@ -317,16 +323,78 @@ def test_grouped_exponentials_random_runs(qi, orc, seed):
 
 def test_window_partition_pass_counts(qi):
     """The fuser's window candidates grow light-cone diamonds on brickwork circuits: the
-    30-qubit, 40-layer benchmark circuit (2260 gates) needs 80 dense blocks and 8 phase
-    polynomials, where the first gate's light-cone block alone needed 141 dense blocks; a
-    bare QFT keeps its 11 dense blocks."""
+    30-qubit, 40-layer benchmark circuit (2260 gates) needs 76 dense blocks, 8 phase
+    polynomials and one qubit permutation (the QFT's 15 closing SWAPs, which filled 4 dense
+    blocks before), where the first gate's light-cone block alone needed 141 dense blocks; a
+    bare QFT takes 6 dense blocks and the permutation."""
     n = 30
     plan = qi.Plan(n, qi.F32, workloads.random_circuit(n, 40, seed=0), fusion=qi.FUSION_GREEDY, max_block_qubits=6)
     ops = plan.ops()
     kinds = [op["kind"] for op in ops]
     # each phase polynomial right after a tensor-core block rides on that block's pass
-    assert kinds.count(4) == 80 and kinds.count(9) + sum("poly" in op for op in ops) == 8
-    assert len(kinds) == 81 + kinds.count(9)
+    assert kinds.count(4) == 76 and kinds.count(9) + sum("poly" in op for op in ops) == 8
+    assert kinds.count(11) == 1 and kinds[-2:] == [11, 8]
+    assert len(kinds) == 78 + kinds.count(9)
     qft = qi.Plan(n, qi.F32, workloads.qft(workloads.GateList(), list(range(n))).array(), fusion=qi.FUSION_GREEDY,
                   max_block_qubits=6)
-    assert [op["kind"] for op in qft.ops()].count(4) <= 11
+    assert [op["kind"] for op in qft.ops()] == [4] * 6 + [11, 8]
+
+
+@pytest.mark.parametrize("kmax", [3, 4, 6])
+@pytest.mark.parametrize("n", [7, 10, 12])
+def test_qft_swap_network_becomes_one_permutation(qi, orc, n, kmax):
+    """The QFT's closing SWAP network (n // 2 swaps across the register) is one qubit
+    permutation op after the fused blocks; replaying the plan matches the oracle."""
+    gl = workloads.GateList()
+    for q in range(n):
+        gl.add("H", [q])
+    workloads.qft(gl, list(range(n)))
+    gates = gl.array()
+    init = workloads.plus_state(n) * np.exp(1j * np.arange(1 << n) * 0.37)
+    init /= np.linalg.norm(init)
+    want = orc.execute(init, n, gates)
+    for prec in (qi.F64, qi.F32):
+        plan = qi.Plan(n, prec, gates, fusion=qi.FUSION_GREEDY, max_block_qubits=kmax)
+        ops = plan.ops()
+        perms = [op for op in ops if op["kind"] == 11]
+        keff = min(kmax, 5) if prec == qi.F64 else kmax   # FP64 blocks stop at 5 qubits
+        assert len(perms) == (1 if n // 2 >= 3 and 2 * (n // 2) > keff else 0)   # the swaps' qubits vs the block size
+        if perms:
+            assert perms[0]["k"] == n // 2 and perms[0]["flip"] == 0
+            assert list(perms[0]["source_bit"]) == list(range(n))[::-1]
+        got = replay(ops, n, init)
+        assert np.max(np.abs(got - want)) < 1e-10
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_swap_x_runs_replay(qi, orc, seed):
+    """Random circuits with runs of long-range SWAPs and X gates between dense layers: runs
+    of three or more SWAPs spanning more than kmax qubits become permutation ops (with the X
+    flips folded in), shorter or narrower runs stay in the fused blocks."""
+    n, kmax = 9, 4
+    rng = np.random.default_rng(seed)
+    gl = workloads.GateList()
+    expect = 0
+    for _ in range(4):
+        for q in range(n):
+            gl.add("RY", [q], [], [float(rng.uniform(0, 6.28))])
+        gl.add("CNOT", [int(rng.integers(1, n))], [0])
+        nsw = int(rng.integers(1, 6))
+        support = set()
+        for _ in range(nsw):
+            a, b = (int(x) for x in rng.choice(n, 2, replace=False))
+            gl.add("SWAP", [a, b])
+            support |= {a, b}
+            if rng.random() < 0.4:
+                t = int(rng.integers(0, n))
+                gl.add("X", [t])
+                support.add(t)
+        expect += nsw >= 3 and len(support) > kmax
+    gates = gl.array()
+    init = workloads.plus_state(n) * np.exp(1j * np.arange(1 << n) * 0.21)
+    init /= np.linalg.norm(init)
+    want = orc.execute(init, n, gates)
+    plan = qi.Plan(n, qi.F64, gates, fusion=qi.FUSION_GREEDY, max_block_qubits=kmax)
+    ops = plan.ops()
+    assert sum(op["kind"] == 11 for op in ops) == expect
+    assert np.max(np.abs(replay(ops, n, init) - want)) < 1e-12

@@ -85,8 +85,9 @@ def test_in_place_fallback_matches(qi):
             hog = torch.empty(free - state_bytes // 2, dtype=torch.uint8, device="cuda")
         try:
             plan.execute(b)
-            got = b.download()
+            b.synchronize()
         finally:
             del hog
             torch.cuda.empty_cache()
+        got = b.download()   # host transfers stage through device memory: after the release
     assert np.array_equal(got, want)

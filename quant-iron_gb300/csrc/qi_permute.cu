@@ -117,11 +117,13 @@ Status affine_gather_async(qi_state *s, void *out, const void *in, const AffineM
 
 // ---------------------------------------------------------------- qubit permutations
 // out[j] = in[s(j)], s(j) = flip ^ sum_k bit k of j << perm[k].  A tile is every index that
-// varies only in the tile bits T = {0..4} (output side) and {k : perm[k] <= 4} (their
-// sources' lowest bits), so both the reads (consecutive source bits 0..4) and the writes
-// (consecutive output bits 0..4) run over 32 consecutive amplitudes; the tile passes
-// through shared memory (one pad slot per 32 entries against bank conflicts).
-constexpr int kPermTileBits = 10;
+// varies only in the tile bits T = {k : k < L or perm[k] < L} (the output's L lowest bits and
+// the outputs whose sources are the source's L lowest bits), so the reads run over 2^L
+// consecutive source amplitudes and the writes over 2^L consecutive output amplitudes; the
+// tile (up to 2^2L amplitudes) passes through shared memory, one pad slot per 2^L entries
+// against bank conflicts.  Per-element offsets come from two tables of 2^L entries (the
+// tile index's low and high L bits).  L = 6 for FP32 (512-byte runs), 5 for FP64.
+constexpr int kPermTileBits = 12;
 struct BitPermParams {
     uint64_t flip;
     uint64_t ntiles;
@@ -133,28 +135,41 @@ struct BitPermParams {
     int8_t perm[64];
 };
 
-__device__ __forceinline__ uint32_t pad32(uint32_t e) { return e + (e >> 5); }
+template <int L> struct PermRun;
+template <> struct PermRun<5> { static constexpr int kTile = 1 << 10; };
+template <> struct PermRun<6> { static constexpr int kTile = 1 << 12; };
 
-template <typename V2>
+template <typename V2, int L>
 __global__ void __launch_bounds__(256) k_bitperm(V2 *__restrict__ out, const V2 *__restrict__ in,
                                                  const __grid_constant__ BitPermParams p) {
-    __shared__ V2 tile[(1 << kPermTileBits) + (1 << kPermTileBits) / 32];
-    __shared__ uint64_t rd_off[1 << kPermTileBits], wr_off[1 << kPermTileBits];
-    __shared__ uint16_t rd_dst[1 << kPermTileBits];
+    constexpr int TMAX = PermRun<L>::kTile, H = 1 << L, U = 4;
+    __shared__ V2 tile[TMAX + TMAX / H];
+    __shared__ uint64_t rd_lo[H], rd_hi[H], wr_lo[H], wr_hi[H];
+    __shared__ uint16_t dst_lo[H], dst_hi[H];
     __shared__ uint64_t dep_j[2 * kAffineMaxBytes][16], dep_s[2 * kAffineMaxBytes][16];   // per 4-bit nibble
-    const int te = 1 << p.nt;
-    for (int e = threadIdx.x; e < te; e += blockDim.x) {
-        uint64_t ro = 0, wo = 0;
-        uint32_t dst = 0;
-        for (int i = 0; i < p.nt; ++i)
-            if ((e >> i) & 1) {
-                ro |= 1ull << p.sbits[i];
-                wo |= 1ull << p.tbits[i];
-                dst |= 1u << p.sdst[i];
+    const int nlo = min(p.nt, L), nhi = p.nt - nlo;
+    for (int v = threadIdx.x; v < H; v += blockDim.x) {
+        uint64_t rl = 0, rh = 0, wl = 0, wh = 0;
+        uint32_t dl = 0, dh = 0;
+        for (int i = 0; i < L; ++i) {
+            if (!((v >> i) & 1)) continue;
+            if (i < nlo) {
+                rl |= 1ull << p.sbits[i];
+                wl |= 1ull << p.tbits[i];
+                dl |= 1u << p.sdst[i];
             }
-        rd_off[e] = ro;
-        wr_off[e] = wo;
-        rd_dst[e] = (uint16_t)pad32(dst);
+            if (i < nhi) {
+                rh |= 1ull << p.sbits[nlo + i];
+                wh |= 1ull << p.tbits[nlo + i];
+                dh |= 1u << p.sdst[nlo + i];
+            }
+        }
+        rd_lo[v] = rl;
+        rd_hi[v] = rh;
+        wr_lo[v] = wl;
+        wr_hi[v] = wh;
+        dst_lo[v] = (uint16_t)dl;
+        dst_hi[v] = (uint16_t)dh;
     }
     // outer index t -> (output base, source base) by one table lookup per nibble of t
     const int nnib = (p.no + 3) / 4;
@@ -172,6 +187,8 @@ __global__ void __launch_bounds__(256) k_bitperm(V2 *__restrict__ out, const V2 
         dep_s[b][v] = ds;
     }
     __syncthreads();
+    const int te = 1 << p.nt, lmask = (1 << nlo) - 1;
+    const int step = blockDim.x;
     for (uint64_t t = blockIdx.x; t < p.ntiles; t += gridDim.x) {
         uint64_t bj = 0, bs = p.flip;
         for (int b = 0; b < nnib; ++b) {
@@ -179,9 +196,27 @@ __global__ void __launch_bounds__(256) k_bitperm(V2 *__restrict__ out, const V2 
             bj |= dep_j[b][v];
             bs ^= dep_s[b][v];
         }
-        for (int e = threadIdx.x; e < te; e += blockDim.x) tile[rd_dst[e]] = in[bs ^ rd_off[e]];
+        for (int e0 = threadIdx.x; e0 < te; e0 += U * step) {   // U gathers in flight per thread
+            V2 v[U];
+            uint32_t d[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const int e = e0 + u * step;
+                if (e < te) {
+                    const int el = e & lmask, eh = e >> nlo;
+                    d[u] = (uint32_t)dst_lo[el] | dst_hi[eh];
+                    v[u] = in[bs ^ rd_lo[el] ^ rd_hi[eh]];
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u)
+                if (e0 + u * step < te) tile[d[u] + (d[u] >> L)] = v[u];
+        }
         __syncthreads();
-        for (int e = threadIdx.x; e < te; e += blockDim.x) out[bj | wr_off[e]] = tile[pad32((uint32_t)e)];
+        for (int e = threadIdx.x; e < te; e += step) {
+            const int el = e & lmask, eh = e >> nlo;
+            out[bj | wr_lo[el] | wr_hi[eh]] = tile[e + (e >> L)];
+        }
         __syncthreads();
     }
 }
@@ -196,9 +231,10 @@ Status bitperm_async(qi_state *s, void *out, const void *in, const int8_t *perm,
         p.perm[k] = perm[k];
         src_of[perm[k]] = k;
     }
+    const int L = s->prec == QI_F32 ? 6 : 5;   // run bits: 512-byte (FP32) / 512-byte (FP64) runs
     bool in_tile[64] = {false};
     for (int k = 0; k < n; ++k)
-        if (k <= 4 || perm[k] <= 4) in_tile[k] = true;
+        if (k < L || perm[k] < L) in_tile[k] = true;
     int tpos[64];
     for (int k = 0; k < n; ++k)
         if (in_tile[k]) {
@@ -218,8 +254,8 @@ Status bitperm_async(qi_state *s, void *out, const void *in, const int8_t *perm,
     p.flip = flip;
     p.ntiles = 1ull << p.no;
     const uint64_t g = std::max<uint64_t>(1, std::min<uint64_t>(p.ntiles, 152 * 4));
-    if (s->prec == QI_F32) k_bitperm<float2><<<(unsigned)g, 256, 0, s->stream>>>((float2 *)out, (const float2 *)in, p);
-    else k_bitperm<double2><<<(unsigned)g, 256, 0, s->stream>>>((double2 *)out, (const double2 *)in, p);
+    if (s->prec == QI_F32) k_bitperm<float2, 6><<<(unsigned)g, 256, 0, s->stream>>>((float2 *)out, (const float2 *)in, p);
+    else k_bitperm<double2, 5><<<(unsigned)g, 256, 0, s->stream>>>((double2 *)out, (const double2 *)in, p);
     count_launch();
     return check_launch("k_bitperm");
 }

@@ -310,15 +310,28 @@ qi_status qi_plan_destroy(qi_plan *p);
  * Circuit::execute (circuit.rs:160-172) and differentiates through the
  * parametric gates (parametric_gate.rs:30-211, Parameter::get parameter.rs:52-57).
  * One forward sweep (fused plan), lambda = H psi, then one reverse sweep in
- * which each gate is un-applied to psi and lambda in a single pass that also
- * accumulates 2 Re<lambda|dU/dtheta|psi> in FP64.  Differentiable kinds: RX,
- * RY, RZ, P, RYPHASE, RYPHASE_DAG, MATCHGATE (any controls).
+ * which gates are un-applied to psi and lambda while 2 Re<lambda|dU/dtheta|psi>
+ * accumulates in FP64: runs of single-qubit gates share one pass, runs of fixed
+ * X / CNOT / SWAP gates are one index permutation, other fixed runs one fused
+ * plan of their inverses, the rest one pass per gate (qi_adjoint_sweep_plan
+ * lists the passes).  Differentiable kinds: RX, RY, RZ, P, RYPHASE,
+ * RYPHASE_DAG, MATCHGATE (any controls).
  * On entry `s` holds |psi0>; on return it holds |psi0> again (restored by the
  * reverse sweep up to rounding).  energy_out (may be NULL) receives E;
  * grads_out[j] = dE/dtheta_j for j < n_theta (parameters that no gate uses get 0). */
 qi_status qi_adjoint_gradient(qi_state *s, const qi_gate *gates, int64_t n_gates, const double *theta,
                               int64_t n_theta, const qi_pauli_term *terms, int64_t n_terms,
                               const qi_exec_options *forward_opts, double *energy_out, double *grads_out);
+/* The passes of qi_adjoint_gradient's reverse sweep for this gate list (host
+ * only, no device work): pass i covers gates hi[i], hi[i] - 1, ..., lo[i] + 1
+ * and is one of 0 one gate (k_adjoint, a per-gate un-apply or a Pauli
+ * exponential), 1 a group of single-qubit gates (k_adjoint_multi), 2 an index
+ * permutation (X / CNOT / SWAP run, k_affine_gather per state), 3 a fused plan
+ * of fixed gates' inverses, 4 identities only.  *n_steps receives the count;
+ * kinds / hi / lo (capacity entries, may all be NULL) receive the passes. */
+qi_status qi_adjoint_sweep_plan(int32_t num_qubits, int32_t precision, const qi_gate *gates, int64_t n_gates,
+                                const double *theta, int64_t n_theta, const qi_exec_options *opts,
+                                int32_t *kinds, int64_t *hi, int64_t *lo, int64_t capacity, int64_t *n_steps);
 
 /* ------------------------------------------------------------------------ */
 /* Measurement (src/components/state.rs:525-784, measurement.rs:15-101)       */

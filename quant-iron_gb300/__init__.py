@@ -411,6 +411,28 @@ def measure_n(state, n_shots, qubits=(), basis="Computational", custom=None, see
     return out[:n_shots]
 
 
+SWEEP_GATE, SWEEP_GROUP, SWEEP_AFFINE, SWEEP_PLAN, SWEEP_SKIP = 0, 1, 2, 3, 4
+
+
+def adjoint_sweep_plan(num_qubits, precision, gates, theta, fusion=FUSION_GREEDY):
+    """The reverse sweep's passes for this gate list (host only): list of (kind, hi, lo), each
+    pass covering gates hi, hi - 1, ..., lo + 1; kinds SWEEP_GATE / GROUP / AFFINE / PLAN / SKIP."""
+    gates = np.ascontiguousarray(gates, dtype=GATE_DTYPE)
+    t = np.ascontiguousarray(theta, dtype=np.float64)
+    opts = _options(fusion, 0, 0)
+    pd = ctypes.POINTER(ctypes.c_double)
+    count = ctypes.c_int64()
+    args = (num_qubits, precision, gates.ctypes.data if gates.size else None, gates.size, t.ctypes.data_as(pd), t.size,
+            ctypes.byref(opts))
+    check(lib.qi_adjoint_sweep_plan(*args, None, None, None, 0, ctypes.byref(count)))
+    kinds = np.zeros(max(1, count.value), dtype=np.int32)
+    hi = np.zeros(max(1, count.value), dtype=np.int64)
+    lo = np.zeros(max(1, count.value), dtype=np.int64)
+    check(lib.qi_adjoint_sweep_plan(*args, kinds.ctypes.data, hi.ctypes.data, lo.ctypes.data, count.value,
+                                    ctypes.byref(count)))
+    return [(int(kinds[i]), int(hi[i]), int(lo[i])) for i in range(count.value)]
+
+
 def adjoint_gradient(state, gates, theta, terms, fusion=FUSION_GREEDY, max_block_qubits=0, use_tensor_cores=0):
     """dE/dtheta of E = <psi(theta)|H|psi(theta)> by one forward and one reverse sweep.
     `state` holds |psi0> before and after the call.  Returns (E, grads)."""

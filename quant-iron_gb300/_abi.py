@@ -209,3 +209,6 @@ lib.qi_plan_op_bitperm.restype = _i32
 lib.qi_plan_op_bitperm.argtypes = [_vp, _i64, _vp, ctypes.POINTER(ctypes.c_uint64)]
 lib.qi_adjoint_gradient.restype = _i32
 lib.qi_adjoint_gradient.argtypes = [_vp, _vp, _i64, _pd, _i64, _vp, _i64, ctypes.POINTER(ExecOptions), _pd, _pd]
+lib.qi_adjoint_sweep_plan.restype = _i32
+lib.qi_adjoint_sweep_plan.argtypes = [_i32, _i32, _vp, _i64, _pd, _i64, ctypes.POINTER(ExecOptions), _vp, _vp, _vp, _i64,
+                                      ctypes.POINTER(_i64)]

@@ -516,6 +516,122 @@ static void fill_adj_positions(AdjParams &p, const GateMatrix &gm, uint64_t cmas
 
 using namespace qi;
 
+// Resolve parameters and build every gate's matrix (whole list first, as the entry point reports
+// the first invalid gate before touching the state).
+static Status resolve_adjoint_gates(int n, const qi_gate *gates, int64_t n_gates, const double *theta, int64_t n_theta,
+                                    std::vector<qi_gate> &resolved, std::vector<GateMatrix> &mats) {
+    resolved.assign((size_t)n_gates, qi_gate());
+    mats.assign((size_t)n_gates, GateMatrix());
+    for (int64_t j = 0; j < n_gates; ++j) {
+        qi_gate g = gates[j];
+        for (int k = 0; k < 3; ++k) {
+            if (g.param_ids[k] >= 0) {
+                if (!theta || g.param_ids[k] >= n_theta)
+                    return err(QI_ERR_MISMATCHED_NUMBER_OF_PARAMETERS, g.param_ids[k] + 1, n_theta);
+                if (!differentiable(g.kind)) return err(QI_ERR_UNSUPPORTED, g.kind, j, "gate kind has no parameter derivative");
+                g.params[k] = theta[g.param_ids[k]];
+            }
+        }
+        if (g.kind == QI_GATE_PAULI_STRING)
+            return err(QI_ERR_UNSUPPORTED, j, -1, "a normalising Pauli-string gate has no inverse");
+        Status st = gate_to_matrix(n, g, &mats[(size_t)j]);
+        if (!st.ok()) return st;
+        resolved[(size_t)j] = g;
+    }
+    return ok_status();
+}
+
+// The reverse sweep as a list of passes, each over gates hi, hi - 1, ..., lo + 1:
+//   kSweepGroup  single-qubit gates with at most one parameter, on at most kMultiQubits qubits
+//                (kMultiQubits - 1 for FP64 states) with at most kMultiStages gates per qubit
+//                (at least two gates): one k_adjoint_multi pass;
+//   kSweepAffine fixed X / CNOT / SWAP gates (at least two that are not identities): one
+//                k_affine_gather per state;
+//   kSweepPlan   other fixed gates (at least two): one fused plan of their inverses per state;
+//   kSweepSkip   fixed identities only;
+//   kSweepGate   one gate on its own (k_adjoint, a per-gate un-apply or a Pauli exponential).
+// Runs of fixed gates become plans or gathers only when fusion is on.
+enum SweepKind : int32_t { kSweepGate = 0, kSweepGroup = 1, kSweepAffine = 2, kSweepPlan = 3, kSweepSkip = 4 };
+struct SweepStep {
+    int32_t kind;
+    int64_t hi, lo;
+};
+
+static std::vector<SweepStep> plan_reverse_sweep(const std::vector<GateMatrix> &mats, const std::vector<qi_gate> &resolved,
+                                                 bool f32, int fusion) {
+    const int64_t n_gates = (int64_t)mats.size();
+    auto n_params = [&](int64_t jj) {
+        int c = 0;
+        for (int k = 0; k < 3; ++k) c += resolved[(size_t)jj].param_ids[k] >= 0;
+        return c;
+    };
+    auto groupable = [&](int64_t jj) {
+        const GateMatrix &m = mats[(size_t)jj];
+        return !m.pauli && m.nt == 1 && m.controls.empty() && n_params(jj) <= 1;
+    };
+    const int max_q = f32 ? kMultiQubits : kMultiQubits - 1;   // FP64 x 16 amplitudes spills
+    std::vector<SweepStep> steps;
+    for (int64_t j = n_gates - 1; j >= 0;) {
+        int qcount[64] = {0};
+        uint64_t qmask = 0;
+        int64_t jj = j;
+        for (; jj >= 0 && groupable(jj); --jj) {
+            const int q = mats[(size_t)jj].t[0];
+            if (!((qmask >> q) & 1ull) && __builtin_popcountll(qmask) == max_q) break;
+            if (qcount[q] == kMultiStages) break;
+            qmask |= 1ull << q;
+            ++qcount[q];
+        }
+        if (j - jj >= 2) {
+            steps.push_back({kSweepGroup, j, jj});
+            j = jj;
+            continue;
+        }
+        for (jj = j; jj >= 0 && n_params(jj) == 0; --jj) {}
+        if (j - jj >= 2 && fusion != QI_FUSION_NONE) {
+            int moves = 0;
+            bool affine = true;
+            for (int64_t k = j; k > jj; --k) {
+                if (mats[(size_t)k].nt == 0 && !mats[(size_t)k].pauli) continue;
+                affine = affine && affine_gate(mats[(size_t)k]);
+                ++moves;
+            }
+            steps.push_back({moves == 0 ? kSweepSkip : (affine && moves >= 2) ? kSweepAffine : kSweepPlan, j, jj});
+            j = jj;
+            continue;
+        }
+        steps.push_back({kSweepGate, j, j - 1});
+        --j;
+    }
+    return steps;
+}
+
+extern "C" qi_status qi_adjoint_sweep_plan(int32_t num_qubits, int32_t precision, const qi_gate *gates, int64_t n_gates,
+                                           const double *theta, int64_t n_theta, const qi_exec_options *opts,
+                                           int32_t *kinds, int64_t *hi, int64_t *lo, int64_t capacity,
+                                           int64_t *n_steps) {
+    if ((!gates && n_gates > 0) || !n_steps) return publish(err(QI_ERR_NULL_ARGUMENT));
+    if (num_qubits <= 0 || num_qubits > 40) return publish(err(QI_ERR_INVALID_NUMBER_OF_QUBITS, num_qubits));
+    if (precision != QI_F32 && precision != QI_F64) return publish(err(QI_ERR_INVALID_INPUT_VALUE, precision));
+    std::vector<qi_gate> resolved;
+    std::vector<GateMatrix> mats;
+    Status st = resolve_adjoint_gates(num_qubits, gates, n_gates, theta, n_theta, resolved, mats);
+    if (!st.ok()) return publish(st);
+    const int fusion = opts ? opts->fusion : QI_FUSION_GREEDY;
+    const std::vector<SweepStep> steps = plan_reverse_sweep(mats, resolved, precision == QI_F32, fusion);
+    *n_steps = (int64_t)steps.size();
+    if (kinds && hi && lo) {
+        if (capacity < (int64_t)steps.size())
+            return publish(err(QI_ERR_INVALID_INPUT_VALUE, capacity, (int64_t)steps.size()));
+        for (size_t i = 0; i < steps.size(); ++i) {
+            kinds[i] = steps[i].kind;
+            hi[i] = steps[i].hi;
+            lo[i] = steps[i].lo;
+        }
+    }
+    return publish(ok_status());
+}
+
 extern "C" qi_status qi_adjoint_gradient(qi_state *s, const qi_gate *gates, int64_t n_gates, const double *theta,
                                          int64_t n_theta, const qi_pauli_term *terms, int64_t n_terms,
                                          const qi_exec_options *forward_opts, double *energy_out, double *grads_out) {
@@ -530,24 +646,11 @@ extern "C" qi_status qi_adjoint_gradient(qi_state *s, const qi_gate *gates, int6
         if (!st.ok()) return publish(st);
     }
     // resolve parameters + validate (whole list first)
-    std::vector<qi_gate> resolved((size_t)n_gates);
-    std::vector<GateMatrix> mats((size_t)n_gates);
-    for (int64_t j = 0; j < n_gates; ++j) {
-        qi_gate g = gates[j];
-        for (int k = 0; k < 3; ++k) {
-            if (g.param_ids[k] >= 0) {
-                if (!theta || g.param_ids[k] >= n_theta)
-                    return publish(err(QI_ERR_MISMATCHED_NUMBER_OF_PARAMETERS, g.param_ids[k] + 1, n_theta));
-                if (!differentiable(g.kind))
-                    return publish(err(QI_ERR_UNSUPPORTED, g.kind, j, "gate kind has no parameter derivative"));
-                g.params[k] = theta[g.param_ids[k]];
-            }
-        }
-        if (g.kind == QI_GATE_PAULI_STRING)
-            return publish(err(QI_ERR_UNSUPPORTED, j, -1, "a normalising Pauli-string gate has no inverse"));
-        Status st = gate_to_matrix(n, g, &mats[(size_t)j]);
+    std::vector<qi_gate> resolved;
+    std::vector<GateMatrix> mats;
+    {
+        Status st = resolve_adjoint_gates(n, gates, n_gates, theta, n_theta, resolved, mats);
         if (!st.ok()) return publish(st);
-        resolved[(size_t)j] = g;
     }
     // forward sweep; the reverse sweep's fixed-gate segments use the same options
     qi_exec_options plan_opts = {QI_FUSION_GREEDY, 0, 0, 0};
@@ -590,35 +693,22 @@ extern "C" qi_status qi_adjoint_gradient(qi_state *s, const qi_gate *gates, int6
     std::vector<std::pair<int64_t, int32_t>> slot_param;   // slot -> parameter id
     int64_t slot = nslots;
     const bool f32 = s->prec == QI_F32;
-    auto n_params = [&](int64_t jj) {
-        int c = 0;
-        for (int k = 0; k < 3; ++k) c += resolved[(size_t)jj].param_ids[k] >= 0;
-        return c;
-    };
-    // a single-qubit, uncontrolled gate with at most one parameter can join a gate group
-    auto groupable = [&](int64_t jj) {
-        const GateMatrix &m = mats[(size_t)jj];
-        return !m.pauli && m.nt == 1 && m.controls.empty() && n_params(jj) <= 1;
-    };
     std::vector<std::unique_ptr<qi_plan>> seg_plans;   // kept until the sweep has run
     void *const psi_home = s->amps;   // psi's own buffer: holds psi again before returning
     void *scratch = nullptr;          // third state buffer for affine gathers (rotates with psi, lambda)
-    for (int64_t j = n_gates - 1; j >= 0 && st.ok();) {
-        // single-qubit gates, consecutive in reverse, on at most kMultiQubits qubits with at
-        // most kMultiStages gates each: one pass for the group
-        int qcount[64] = {0};
-        uint64_t qmask = 0;
-        int64_t jj = j;
-        const int max_q = f32 ? kMultiQubits : kMultiQubits - 1;   // FP64 x 16 amplitudes spills
-        for (; jj >= 0 && groupable(jj); --jj) {
-            const int q = mats[(size_t)jj].t[0];
-            if (!((qmask >> q) & 1ull) && __builtin_popcountll(qmask) == max_q) break;
-            if (qcount[q] == kMultiStages) break;
-            qmask |= 1ull << q;
-            ++qcount[q];
-        }
-        const int64_t gsize = j - jj;
-        if (gsize >= 2) {
+    const std::vector<SweepStep> steps = plan_reverse_sweep(mats, resolved, f32, plan_opts.fusion);
+    for (size_t si = 0; si < steps.size() && st.ok(); ++si) {
+        const int64_t j = steps[si].hi, jj = steps[si].lo;
+        const int32_t kind = steps[si].kind;
+        if (kind == kSweepSkip) continue;
+        if (kind == kSweepGroup) {   // gates j .. jj + 1: one k_adjoint_multi pass
+            int qcount[64] = {0};
+            uint64_t qmask = 0;
+            for (int64_t k = j; k > jj; --k) {
+                const int q = mats[(size_t)k].t[0];
+                qmask |= 1ull << q;
+                ++qcount[q];
+            }
             MultiParams mp;
             std::memset(&mp, 0, sizeof(mp));
             const int M = __builtin_popcountll(qmask);
@@ -691,42 +781,31 @@ extern "C" qi_status qi_adjoint_gradient(qi_state *s, const qi_gate *gates, int6
             count_launch(2);
             st = check_launch("k_finalize_to");
             for (auto &cp : comp_param) slot_param.push_back({slot + cp.first, cp.second});
-            j = jj;
             continue;
         }
-        // fixed gates, consecutive in reverse: their inverses as one fused plan on psi and lambda
-        for (jj = j; jj >= 0 && n_params(jj) == 0; --jj) {}
-        if (j - jj >= 2 && plan_opts.fusion != QI_FUSION_NONE) {
-            // only X / CNOT / SWAP: one index permutation per state, out[x] = in[f(x)] with f
-            // the run's forward map (gathering through f un-applies the run)
-            int moves = 0;
-            bool affine = true;
-            for (int64_t k = j; k > jj; --k) {
-                if (mats[(size_t)k].nt == 0) continue;
-                affine = affine && affine_gate(mats[(size_t)k]);
-                ++moves;
-            }
-            if (affine && moves >= 2) {
-                AffineMap am;
-                affine_identity(am);
-                for (int64_t k = jj + 1; k <= j; ++k)
-                    if (mats[(size_t)k].nt != 0) affine_compose(am, mats[(size_t)k]);
-                if (!scratch) {
-                    e = cudaMalloc(&scratch, s->bytes());
-                    if (e != cudaSuccess) {
-                        scratch = nullptr;
-                        st = cuda_status(e, "cudaMalloc(permutation buffer)");
-                        break;
-                    }
+        if (kind == kSweepAffine) {
+            // X / CNOT / SWAP only: one index permutation per state, out[x] = in[f(x)] with f the
+            // run's forward map (gathering through f un-applies the run)
+            AffineMap am;
+            affine_identity(am);
+            for (int64_t k = jj + 1; k <= j; ++k)
+                if (mats[(size_t)k].nt != 0) affine_compose(am, mats[(size_t)k]);
+            if (!scratch) {
+                e = cudaMalloc(&scratch, s->bytes());
+                if (e != cudaSuccess) {
+                    scratch = nullptr;
+                    st = cuda_status(e, "cudaMalloc(permutation buffer)");
+                    break;
                 }
-                for (qi_state *q : {s, lam}) {
-                    st = affine_gather_async(s, scratch, q->amps, am);
-                    if (!st.ok()) break;
-                    std::swap(q->amps, scratch);
-                }
-                j = jj;
-                continue;
             }
+            for (qi_state *q : {s, lam}) {
+                st = affine_gather_async(s, scratch, q->amps, am);
+                if (!st.ok()) break;
+                std::swap(q->amps, scratch);
+            }
+            continue;
+        }
+        if (kind == kSweepPlan) {   // fixed gates: their inverses as one fused plan on psi and lambda
             std::vector<Elem> inv;
             for (int64_t k = j; k > jj; --k) {
                 GateMatrix gi = mats[(size_t)k];
@@ -740,10 +819,7 @@ extern "C" qi_status qi_adjoint_gradient(qi_state *s, const qi_gate *gates, int6
                 }
                 inv.push_back(make_elem_from_gate(gi, (int)inv.size()));
             }
-            if (inv.empty()) {   // identities only
-                j = jj;
-                continue;
-            }
+            if (inv.empty()) continue;   // identities only (planned as kSweepSkip)
             std::unique_ptr<qi_plan> seg(new qi_plan());
             seg->n = n;
             seg->prec = s->prec;
@@ -754,12 +830,11 @@ extern "C" qi_status qi_adjoint_gradient(qi_state *s, const qi_gate *gates, int6
             if (st.ok()) st = plan_execute(seg.get(), s);
             if (st.ok()) st = plan_execute(seg.get(), lam);
             seg_plans.push_back(std::move(seg));
-            j = jj;
             continue;
         }
+        // kSweepGate: gate j on its own
         const GateMatrix &gm = mats[(size_t)j];
         const qi_gate &g = resolved[(size_t)j];
-        --j;
         int ids[3], nd = 0;
         for (int k = 0; k < 3; ++k)
             if (g.param_ids[k] >= 0) ids[nd++] = k;

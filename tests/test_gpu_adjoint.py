@@ -226,3 +226,36 @@ def test_permutation_runs_in_reverse_sweep(qi, orc, layers, prec):
         ids = list(range(0, npar, 7))
         g_ref = fd_grad(orc, n, gl.array(), theta, terms, init, ids)
         assert np.linalg.norm(g1[ids] - g_ref) / np.linalg.norm(g_ref) < 1e-6
+
+
+@pytest.mark.parametrize("prec", [0, 1], ids=["f64", "f32"])
+def test_pauli_exponential_inside_a_cnot_swap_run(qi, orc, prec):
+    """A fixed run of CNOT / SWAP gates with a Pauli exponential inside is un-applied as a
+    fused plan (an index permutation would drop the exponential): gradients equal the
+    per-gate sweep and FP64 finite differences."""
+    n = 8
+    gl = workloads.GateList()
+    npar = 0
+    for rep in range(2):
+        for q in range(n):
+            gl.add("RY", [q], [], [0.0], [npar])
+            npar += 1
+        gl.add("CNOT", [1], [0]).add("SWAP", [2, 6])
+        gl.add("PAULI_EVOLUTION", [], [], [0.7, 0.0, 0.3 + rep], xmask=0b1010, zmask=0b0110)
+        gl.add("CNOT", [5], [4]).add("SWAP", [3, 7])
+    gates = gl.array()
+    theta = np.linspace(-1.2, 1.4, npar)
+    assert any(k == qi.SWEEP_PLAN for k, _, _ in qi.adjoint_sweep_plan(n, prec, gates, theta))
+    terms = workloads.xxz_periodic(n, seed=5)
+    init = workloads.plus_state(n)
+    res = {}
+    for fusion in (qi.FUSION_NONE, qi.FUSION_GREEDY):
+        with qi.DeviceState(n, prec) as st:
+            st.upload(init)
+            res[fusion] = qi.adjoint_gradient(st, gates, theta, terms, fusion=fusion)[1]
+    g0, g1 = res[qi.FUSION_NONE], res[qi.FUSION_GREEDY]
+    assert np.linalg.norm(g1 - g0) / np.linalg.norm(g0) < (1e-10 if prec == 0 else 1e-4)
+    if prec == 0:
+        ids = list(range(npar))
+        g_ref = fd_grad(orc, n, gates, theta, terms, init, ids)
+        assert np.linalg.norm(g1 - g_ref) / np.linalg.norm(g_ref) < 1e-6

@@ -534,8 +534,9 @@ def main():
             st2 = qi.DeviceState(n, qi.F32)
             st2.set_stream(stream2.cuda_stream)
             states = [st, st2]
-            for s2 in states:   # allocates each state's staging buffer (an allocation synchronises the device)
-                s2.upload_async(host_in.data_ptr(), dim)
+            for s2 in states:   # allocates each state's staging and second buffers (an allocation synchronises
+                s2.upload_async(host_in.data_ptr(), dim)   # the device, so none may happen in the timed loop)
+                plan.execute(s2)
                 s2.synchronize()
         torch.cuda.synchronize()
         t0 = time.perf_counter()

@@ -24,6 +24,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
@@ -65,7 +66,8 @@ class ClockSampler:
     def __init__(self, device_index):
         self.dev = device_index
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", "clocks_bench.csv")
+        self.path = os.environ.get("QI_BENCH_CLOCKS_CSV",
+                                   os.path.join(tempfile.gettempdir(), "qi_bench_clocks_%d.csv" % os.getpid()))
 
     def start(self):
         try:

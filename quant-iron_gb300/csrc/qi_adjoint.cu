@@ -783,29 +783,28 @@ extern "C" qi_status qi_adjoint_gradient(qi_state *s, const qi_gate *gates, int6
             for (auto &cp : comp_param) slot_param.push_back({slot + cp.first, cp.second});
             continue;
         }
+        bool as_plan = kind == kSweepPlan;
         if (kind == kSweepAffine) {
             // X / CNOT / SWAP only: one index permutation per state, out[x] = in[f(x)] with f the
             // run's forward map (gathering through f un-applies the run)
-            AffineMap am;
-            affine_identity(am);
-            for (int64_t k = jj + 1; k <= j; ++k)
-                if (mats[(size_t)k].nt != 0) affine_compose(am, mats[(size_t)k]);
-            if (!scratch) {
-                e = cudaMalloc(&scratch, s->bytes());
-                if (e != cudaSuccess) {
-                    scratch = nullptr;
-                    st = cuda_status(e, "cudaMalloc(permutation buffer)");
-                    break;
+            if (!scratch && cudaMalloc(&scratch, s->bytes()) != cudaSuccess) {
+                scratch = nullptr;
+                cudaGetLastError();   // no room for a third state buffer: un-apply the run as a plan
+                as_plan = true;
+            } else {
+                AffineMap am;
+                affine_identity(am);
+                for (int64_t k = jj + 1; k <= j; ++k)
+                    if (mats[(size_t)k].nt != 0) affine_compose(am, mats[(size_t)k]);
+                for (qi_state *q : {s, lam}) {
+                    st = affine_gather_async(s, scratch, q->amps, am);
+                    if (!st.ok()) break;
+                    std::swap(q->amps, scratch);
                 }
+                continue;
             }
-            for (qi_state *q : {s, lam}) {
-                st = affine_gather_async(s, scratch, q->amps, am);
-                if (!st.ok()) break;
-                std::swap(q->amps, scratch);
-            }
-            continue;
         }
-        if (kind == kSweepPlan) {   // fixed gates: their inverses as one fused plan on psi and lambda
+        if (as_plan) {   // fixed gates: their inverses as one fused plan on psi and lambda
             std::vector<Elem> inv;
             for (int64_t k = j; k > jj; --k) {
                 GateMatrix gi = mats[(size_t)k];

@@ -145,3 +145,25 @@ def test_pauli_exponential_breaks_a_permutation_run(qi):
     gl2.add("IDENTITY", [2]).add("IDENTITY", [4]).add("IDENTITY", [3])
     steps2 = qi.adjoint_sweep_plan(6, 1, gl2.array(), np.array([0.2]))
     assert steps2[0][0] == qi.SWEEP_AFFINE and steps2[0][1:] == (6, 0)
+
+
+def test_sweep_plan_errors(qi):
+    """The introspection validates like qi_adjoint_gradient: parameter ids past theta, a
+    non-differentiable parametric kind, a normalising Pauli string, bad qubit counts."""
+    gl = workloads.GateList().add("RY", [0], [], [0.0], [3])
+    with pytest.raises(qi.QuantIronError) as ei:
+        qi.adjoint_sweep_plan(2, 1, gl.array(), np.zeros(2))
+    assert ei.value.variant == "MismatchedNumberOfParameters"
+    gl = workloads.GateList().add("H", [0], [], [], [0])
+    with pytest.raises(qi.QuantIronError) as ei:
+        qi.adjoint_sweep_plan(2, 1, gl.array(), np.zeros(1))
+    assert ei.value.variant == "Unsupported"
+    gl = workloads.GateList().add("PAULI_STRING", [], [], [1.0, 0.0], xmask=1, zmask=0)
+    with pytest.raises(qi.QuantIronError) as ei:
+        qi.adjoint_sweep_plan(2, 1, gl.array(), np.zeros(1))
+    assert ei.value.variant == "Unsupported"
+    for nq in (0, 41):
+        with pytest.raises(qi.QuantIronError) as ei:
+            qi.adjoint_sweep_plan(nq, 1, workloads.GateList().array(), np.zeros(1))
+        assert ei.value.variant == "InvalidNumberOfQubits"
+    assert qi.adjoint_sweep_plan(3, 0, workloads.GateList().array(), np.zeros(1)) == []

@@ -10,10 +10,19 @@ One step = one execution of the whole circuit on the resident state
 layers/s (40 layers per step).  Inputs (8 GiB of FP32 amplitudes) are far
 larger than the 129 MB L2, so no L2 flush is needed between steps.
 
-Besides the JSON keys the contract requires, the line carries the plain FP64
-per-gate CUDA path (the >= 8x target's denominator), the complex-FP32
-per-gate path, and the fused path's infidelity against the FP64 per-gate
-result (FP64 accumulation on the device).
+Besides the JSON keys the contract requires, the line carries the other
+configurations of the workload family, each against an FP64 result on the device:
+  seeds       the 30-qubit circuit on seeds 0-4: fused FP32 against the plain FP64
+              per-gate path (the >= 8x target's denominator), infidelity, full-state
+              max amplitude error, energy error, both times;
+  per_gate    one kernel per gate by kind and target qubit, FP32 and FP64, as a
+              fraction of the measured copy bandwidth;
+  adjoint     26-qubit hardware-efficient ansatz gradient (624 parameters): FP32
+              gradients/s, FP32 vs FP64 adjoint, FP64 central differences and
+              parameter shift (seeded subsets; --adjoint-fd all for every parameter);
+  trotter     100 first-order Trotter steps on the 5x6 lattice, Heisenberg and TFIM,
+              FP32 fused vs FP64 grouped, <H> every 10 steps;
+  e2e         the same circuit through the public API from and to host buffers.
 
 --impl reference times the reference implementation's CPU data flow (the
 oracle port of the rayon branch, oracle/qi_oracle.cpp) on a bounded sample.
@@ -44,6 +53,8 @@ def parse():
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
     ap.add_argument("--qubits", type=int, default=N_QUBITS)
     ap.add_argument("--skip-baselines", action="store_true", help="skip FP64/FP32 per-gate and CPU legs")
+    ap.add_argument("--adjoint-fd", default="subset", choices=["subset", "all"],
+                    help="finite differences / parameter shift on a seeded subset (64 / 32 parameters) or on all 624")
     ap.add_argument("--profile-case", default=None, choices=["fused26", "trotter26", "adjoint26"],
                     help="run a small fixed case for ncu captures instead of the benchmark")
     return ap.parse_args()
@@ -106,16 +117,83 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_port_sample(n, gates, budget_gates, threads):
-    """Time the oracle port of the reference's rayon data flow on the first
-    `budget_gates` gates at n qubits; returns (seconds per gate, gates timed, n)."""
+def load_workloads():
+    """The package's workload generators without the engine library: a stand-in package
+    object whose __init__ (which loads libqi_gb300.so) is never run, so the reference arm
+    maps no engine code."""
+    import importlib
+    import types
+    name = "_qi_workloads_only"
+    if name not in sys.modules:
+        pkg = types.ModuleType(name)
+        pkg.__path__ = [os.path.join(ROOT, "quant-iron_gb300")]
+        sys.modules[name] = pkg
+    return importlib.import_module(name + ".workloads")
+
+
+GATE_CLASSES = ("1q diagonal", "1q pair", "CNOT", "controlled phase", "SWAP", "other")
+
+
+def gate_class(g, kinds):
+    k = int(g["kind"])
+    nc = int(g["n_controls"])
+    if k == kinds["SWAP"]:
+        return "SWAP"
+    if k == kinds["CNOT"]:
+        return "CNOT"
+    if k in (kinds["Z"], kinds["S"], kinds["T"], kinds["SDAG"], kinds["TDAG"], kinds["P"], kinds["RZ"],
+             kinds["IDENTITY"]):
+        return "controlled phase" if nc else "1q diagonal"
+    if k in (kinds["H"], kinds["X"], kinds["Y"], kinds["RX"], kinds["RY"], kinds["U2"]) and nc == 0:
+        return "1q pair"
+    return "other"
+
+
+def reference_cpu_sample(n, gates, kinds, warm, samples, threads):
+    """The oracle port of the reference's rayon data flow (clone + per-pair update list +
+    serial scatter, on `threads` host threads) timed gate by gate on a stratified sample of
+    the circuit: sample k is a gate of class k mod 5 (1q diagonal, 1q pair, CNOT,
+    controlled phase, SWAP), taken at a seeded position among that class's gates; the
+    `warm` untimed gates come first.  The whole circuit's time is estimated as
+    sum over classes of (gates in the class x mean sampled time of the class).
+    Returns (estimated seconds per circuit, per-sample seconds, description)."""
     import numpy as np
     from oracle import oracle as orc
-    from quant_iron_gb300 import workloads
-    init = workloads.plus_state(n)
-    _, secs = orc.port_execute(init, n, gates[:budget_gates], threads)
+    by_class = {}
+    for i in range(gates.size):
+        by_class.setdefault(gate_class(gates[i], kinds), []).append(i)
+    order = [c for c in GATE_CLASSES if c in by_class]
+    rng = np.random.default_rng(12345)
+    picks = []
+    for k in range(warm + samples):
+        c = order[k % len(order)]
+        picks.append((c, by_class[c][int(rng.integers(0, len(by_class[c])))]))
+    init = np.full(1 << n, 1.0 / np.sqrt(1 << n), dtype=np.complex128)
+    _, secs = orc.port_execute_timed(init, n, gates[[i for _, i in picks]], threads)
     del init
-    return secs / budget_gates
+    timed = list(zip([c for c, _ in picks[warm:]], secs[warm:]))
+    mean_all = float(np.mean([t for _, t in timed])) if timed else 0.0
+    per_class = {}
+    for c in order:
+        ts = [t for cc, t in timed if cc == c]
+        per_class[c] = {"gates": len(by_class[c]), "sampled": len(ts),
+                        "mean_s": float(np.mean(ts)) if ts else mean_all}
+    est = sum(v["gates"] * v["mean_s"] for v in per_class.values())
+    desc = ("oracle port of the reference rayon data flow (clone + per-pair update list + serial scatter) on %d "
+            "host threads, %d qubits: %d gates timed one by one (stratified over the gate classes, %d warm-up "
+            "gates untimed); circuit time = sum over classes of count x mean sampled time, extrapolation "
+            "factor %.1f (%d gates / %d timed)" % (threads, n, len(timed), warm, gates.size / max(1, len(timed)),
+                                                     gates.size, len(timed)))
+    return est, [float(t) for _, t in timed], per_class, desc
+
+
+def workload_config(n, gates, world):
+    """The `config` both arms print (the same workload, whatever implements it)."""
+    return {"workload": "random circuit, %d qubits, %d layers + QFT (%d gates), |+>^%d, seed %d" %
+                        (n, LAYERS, gates.size, n, SEED),
+            "qubits": n, "layers": LAYERS, "gates": int(gates.size),
+            "l2": "inputs (%.3g GiB FP32 state) larger than the 129 MB L2; no flush" % ((1 << n) * 8 / 2**30),
+            "parallelism": "replicas" if world > 1 else "single GPU"}
 
 
 def replica_throughput(ms, world, steps, device="cuda"):
@@ -140,41 +218,75 @@ def host_mem_gb():
     return 0.0
 
 
-def cpu_baseline(n, gates, budget_s=25.0):
-    """Bounded sample of the reference CPU data flow; picks the gate count to stay near budget_s."""
+def cpu_baseline(n, gates, kinds):
+    """Bounded sample (one gate per class, about 20 s at 30 qubits) of the reference CPU data flow."""
     threads = os.cpu_count() or 1
-    # the rayon data flow holds ~56 B/amp (state, clone, update list); fall back to fewer qubits if short
-    need_gb = (1 << n) * 60 / 1e9
     nn = n
-    while nn > 20 and host_mem_gb() < need_gb * 1.3:
+    while nn > 20 and host_mem_gb() < (1 << nn) * 60 / 1e9 * 1.3:   # the rayon data flow holds ~56 B/amp
         nn -= 1
-        need_gb = (1 << nn) * 60 / 1e9
-    from quant_iron_gb300 import workloads
-    g = gates if nn == n else workloads.random_circuit(nn, LAYERS, seed=SEED)
-    t1 = cpu_port_sample(nn, g, 1, threads)
-    k = max(1, min(len(g) - 1, int(budget_s / max(t1, 1e-6)) - 1))
-    tk = cpu_port_sample(nn, g[1:], k, threads) if k > 0 else t1
-    per_gate = tk * (1 << (n - nn))   # scale a smaller sample to n qubits by amplitude count
-    step_s = per_gate * len(gates)
-    return {"value": LAYERS / step_s, "unit": "layers/s", "cores": threads, "kind": "port",
-            "sample": "oracle port of the reference rayon data flow (clone + per-pair update list + serial "
-                      "scatter): %d gates of the %d-qubit circuit timed, extrapolated to all %d gates%s" %
-                      (k + 1, nn, len(gates), "" if nn == n else " and scaled by 2^%d amplitudes" % (n - nn)),
-            "seconds_per_gate": per_gate}
+    g = gates if nn == n else load_workloads().random_circuit(nn, LAYERS, seed=SEED)
+    est, _, per_class, desc = reference_cpu_sample(nn, g, kinds, 0, 5, threads)
+    est *= float(1 << (n - nn))   # a smaller sample scaled to n qubits by amplitude count
+    if nn != n:
+        desc += "; scaled by 2^%d amplitudes to %d qubits" % (n - nn, n)
+    return {"value": LAYERS / est, "unit": "layers/s", "cores": threads, "kind": "port", "sample": desc,
+            "seconds_per_circuit": est, "classes": per_class}
 
 
-def adjoint_leg(qi, workloads, stream, torch, np, n=26, layers=12):
+def fd_energies(qi, n, gates, theta, terms, ids, shifts, stream):
+    """E(theta + s e_j) for every parameter j in ids and shift s, with the plain FP64 per-gate
+    path: the state after each 77-gate layer of the unshifted circuit is kept (FP64), so an
+    evaluation runs from the checkpoint before the shifted gate's layer to the end.
+    Returns {(j, s): E}."""
+    import numpy as np
+    layer_len = 3 * n - 1
+    n_layers = gates.size // layer_len
+    ck = []
+    st = qi.DeviceState(n, qi.F64)
+    st.set_stream(stream.cuda_stream)
+    st.set_zero()
+    for layer in range(n_layers):
+        c = qi.DeviceState(n, qi.F64)
+        c.set_stream(stream.cuda_stream)
+        c.copy_from(st)
+        ck.append(c)
+        qi.Plan(n, qi.F64, gates[layer * layer_len:(layer + 1) * layer_len], theta=theta,
+                fusion=qi.FUSION_NONE).execute(st)
+    pid_layer = {}
+    for pos in range(gates.size):
+        for k in range(3):
+            pid = int(gates[pos]["param_ids"][k])
+            if pid >= 0:
+                pid_layer[pid] = pos // layer_len
+    out = {}
+    for j in ids:
+        layer = pid_layer[int(j)]
+        tail = gates[layer * layer_len:]
+        for sgn in shifts:
+            th = theta.copy()
+            th[j] += sgn
+            st.copy_from(ck[layer])
+            qi.Plan(n, qi.F64, tail, theta=th, fusion=qi.FUSION_NONE).execute(st)
+            out[(int(j), sgn)] = qi.sumop_expectation(st, terms).real
+    for c in ck:
+        c.close()
+    st.close()
+    return out
+
+
+def adjoint_leg(qi, workloads, stream, torch, np, n=26, layers=12, fd="subset"):
     """Adjoint gradient of the 26-qubit hardware-efficient ansatz (12 layers of RY.RZ + CNOT
-    ladder, 624 parameters, seed 1) on the periodic XXZ energy: gradients/s with an FP32
-    state, agreement with the FP64-state adjoint, and FP64 central differences (eps 1e-4)
-    on 8 seeded parameters."""
+    ladder, 624 parameters, seed 1) on the periodic XXZ energy (104 terms): gradients/s with an
+    FP32 state; the FP32 and FP64 adjoints on all 624 parameters; FP64 central differences
+    (eps 1e-4) and parameter shift (+-pi/2) from the plain FP64 per-gate path, on a seeded
+    subset (fd="subset": 64 and 32 parameters) or on every parameter (fd="all")."""
     gates, theta = workloads.hea_ansatz(n, layers, seed=1)
     terms = workloads.xxz_periodic(n, seed=1)
     s32 = qi.DeviceState(n, qi.F32)
     s32.set_stream(stream.cuda_stream)
     s32.set_zero()
     qi.adjoint_gradient(s32, gates, theta, terms)   # warm-up
-    reps = 3
+    reps = 5
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(reps):
@@ -185,111 +297,193 @@ def adjoint_leg(qi, workloads, stream, torch, np, n=26, layers=12):
     s64 = qi.DeviceState(n, qi.F64)
     s64.set_stream(stream.cuda_stream)
     s64.set_zero()
-    e64, g64 = qi.adjoint_gradient(s64, gates, theta, terms)
-    rel32 = float(np.linalg.norm(g32 - g64) / np.linalg.norm(g64))
-    # FP64 central differences with the plain per-gate FP64 path
-    rng = np.random.default_rng(1)
-    ids = rng.choice(theta.size, 8, replace=False)
-    fd = []
-    for j in ids:
-        vals = []
-        for sgn in (1, -1):
-            th = theta.copy()
-            th[j] += sgn * 1e-4
-            s64.set_zero()
-            qi.Plan(n, qi.F64, gates, theta=th, fusion=qi.FUSION_NONE).execute(s64)
-            vals.append(qi.sumop_expectation(s64, terms).real)
-        fd.append((vals[0] - vals[1]) / 2e-4)
-    fd = np.array(fd)
-    rel_fd = float(np.linalg.norm(g64[ids] - fd) / np.linalg.norm(fd))
-    rel_fd32 = float(np.linalg.norm(g32[ids] - fd) / np.linalg.norm(fd))
-    s64.close()
-    return {"workload": "HEA %d qubits, %d layers, %d parameters, periodic XXZ (%d terms)" % (n, layers, theta.size,
-                                                                                             len(terms)),
-            "grad_per_s_fp32": 1.0 / t_adj, "seconds_per_grad_fp32": t_adj, "energy_fp32": e32, "energy_fp64": e64,
-            "rel_err_fp32_vs_fp64_adjoint": rel32, "rel_err_fp64_adjoint_vs_fd_subset": rel_fd,
-            "rel_err_fp32_adjoint_vs_fd_subset": rel_fd32, "fd_subset": [int(x) for x in ids]}
-
-
-def trotter_leg(qi, workloads, stream, torch, np, rows=5, cols=6, steps=20, observe_every=10):
-    """First-order Trotter evolution on the 5x6 open lattice (30 qubits): anisotropic
-    Heisenberg (1.0 XX + 0.8 YY + 0.5 ZZ per bond, h_i Z_i), 177 terms, dt = 0.05, from a
-    seeded basis state.  The FP32 fused step (one plan per step, <H> every 10 steps) is
-    timed over `steps` steps; the FP64 step (grouped exponentials: one pass per run of
-    terms whose X-masks lie in {0, X}, i.e. one per bond plus the field run) is timed
-    over 2 steps, and <H> after 2 steps of both is compared."""
-    n = rows * cols
-    terms = workloads.lattice_xyz(rows, cols, seed=0)
-    basis = int(np.random.default_rng(0).integers(0, 1 << n))
-    out = {"workload": "5x6 lattice anisotropic Heisenberg, %d terms, dt 0.05, basis state %d" % (len(terms), basis),
-           "steps": steps}
-    s32 = qi.DeviceState(n, qi.F32)
-    s32.set_stream(stream.cuda_stream)
-    s32.set_basis(basis)
-    qi.trotter_evolve(s32, terms, 0.05, 2)   # warm-up (plan build, first launches)
-    e32_2 = qi.sumop_expectation(s32, terms).real
-    s32.set_basis(basis)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    e32 = qi.trotter_evolve(s32, terms, 0.05, steps, observable=terms, observe_every=observe_every)
-    t32 = time.perf_counter() - t0
-    s32.close()
+    e64, g64 = qi.adjoint_gradient(s64, gates, theta, terms)
+    t64 = time.perf_counter() - t0
+    s64.close()
+    rng = np.random.default_rng(1)
+    if fd == "all":
+        fd_ids = np.arange(theta.size)
+        ps_ids = np.arange(theta.size)
+    else:
+        fd_ids = np.sort(rng.choice(theta.size, 64, replace=False))
+        ps_ids = np.sort(rng.choice(theta.size, 32, replace=False))
+    t0 = time.perf_counter()
+    ev = fd_energies(qi, n, gates, theta, terms, fd_ids, (1e-4, -1e-4), stream)
+    ev.update(fd_energies(qi, n, gates, theta, terms, ps_ids, (np.pi / 2, -np.pi / 2), stream))
+    t_ref = time.perf_counter() - t0
+    g_fd = np.array([(ev[(int(j), 1e-4)] - ev[(int(j), -1e-4)]) / 2e-4 for j in fd_ids])
+    g_ps = np.array([(ev[(int(j), np.pi / 2)] - ev[(int(j), -np.pi / 2)]) / 2 for j in ps_ids])
+
+    def rel(a, b):
+        return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+    comp = np.abs(g32[fd_ids] - g_fd) / np.maximum(np.abs(g_fd), 1e-300)
+    return {"workload": "HEA %d qubits, %d layers, %d parameters, periodic XXZ (%d terms), |0>" %
+                        (n, layers, theta.size, len(terms)),
+            "grad_per_s_fp32": 1.0 / t_adj, "seconds_per_grad_fp32": t_adj, "seconds_per_grad_fp64": t64,
+            "energy_fp32": e32, "energy_fp64": e64, "energy_error_fp32": abs(e32 - e64),
+            "rel_err_fp32_vs_fp64_adjoint_all": rel(g32, g64),
+            "fd": {"eps": 1e-4, "parameters": int(fd_ids.size), "source": "plain FP64 per-gate path, per-layer "
+                                                                           "FP64 checkpoints",
+                   "rel_err_fp32_adjoint": rel(g32[fd_ids], g_fd), "rel_err_fp64_adjoint": rel(g64[fd_ids], g_fd),
+                   "max_componentwise_rel_err_fp32": float(np.max(comp)),
+                   "median_componentwise_rel_err_fp32": float(np.median(comp))},
+            "parameter_shift": {"parameters": int(ps_ids.size), "rel_err_fp32_adjoint": rel(g32[ps_ids], g_ps),
+                                "rel_err_fp64_adjoint": rel(g64[ps_ids], g_ps)},
+            "reference_seconds": t_ref,
+            "norm_grad_fp64": float(np.linalg.norm(g64))}
+
+
+def trotter_leg(qi, workloads, stream, torch, np, rows=5, cols=6, steps=100, observe_every=10):
+    """First-order Trotter evolution on the 5x6 open lattice (30 qubits), dt = 0.05, from a
+    seeded basis state, for the anisotropic Heisenberg SumOp (1.0 XX + 0.8 YY + 0.5 ZZ per bond,
+    h_i Z_i; 177 terms) and the transverse-field Ising SumOp (-J_ij ZZ - g X_i, J ~ U(0.5, 1.5),
+    g = 1; 79 terms).  `steps` steps of the FP32 fused method (one plan per step) and of the
+    FP64 grouped method (one pass per run of terms with X-masks in {0, X}), <H> in FP64
+    every `observe_every` steps for both; the energy-error trajectory FP32 - FP64."""
+    n = rows * cols
+    basis = int(np.random.default_rng(0).integers(0, 1 << n))
+    out = {"lattice": "%dx%d open, site r*%d + c" % (rows, cols, cols), "dt": 0.05, "steps": steps,
+           "observe_every": observe_every, "basis_state": basis}
+    for name, terms in (("heisenberg", workloads.lattice_xyz(rows, cols, seed=0)),
+                        ("tfim", workloads.lattice_tfim(rows, cols, seed=0))):
+        res = {"terms": len(terms)}
+        for label, prec in (("fp32_fused", qi.F32), ("fp64_grouped", qi.F64)):
+            st = qi.DeviceState(n, prec)
+            st.set_stream(stream.cuda_stream)
+            st.set_basis(basis)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            e = qi.trotter_evolve(st, terms, 0.05, steps, observable=terms, observe_every=observe_every)
+            torch.cuda.synchronize()
+            dt = time.perf_counter() - t0
+            st.close()
+            res[label] = {"ms_per_step": dt * 1e3 / steps, "energies": [complex(x).real for x in e]}
+        e32 = np.array(res["fp32_fused"]["energies"])
+        e64 = np.array(res["fp64_grouped"]["energies"])
+        res["energy_error"] = [float(x) for x in np.abs(e32 - e64)]
+        res["max_energy_error"] = float(np.max(np.abs(e32 - e64)))
+        res["speedup_fp32_fused_vs_fp64_grouped"] = (res["fp64_grouped"]["ms_per_step"] /
+                                                     res["fp32_fused"]["ms_per_step"])
+        out[name] = res
+    out["note"] = "timed regions include the <H> evaluations"
+    return out
+
+
+def seeds_leg(qi, workloads, stream, torch, n, seeds, terms):
+    """The benchmark circuit family at n qubits for several seeds: the fused complex-FP32 plan
+    against the plain FP64 per-gate plan on the device — infidelity, full-state max amplitude
+    error (every one of the 2^n amplitudes) and energy error (<H> of the open-chain
+    Heisenberg, FP64 reductions) — with both methods' times."""
+    out = []
     s64 = qi.DeviceState(n, qi.F64)
     s64.set_stream(stream.cuda_stream)
-    s64.set_basis(basis)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    qi.trotter_evolve(s64, terms, 0.05, 2)
-    t64_step = (time.perf_counter() - t0) / 2
-    e64_2 = qi.sumop_expectation(s64, terms).real
+    s32 = qi.DeviceState(n, qi.F32)
+    s32.set_stream(stream.cuda_stream)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for seed in seeds:
+        gates = workloads.random_circuit(n, LAYERS, seed=seed)
+        p64 = qi.Plan(n, qi.F64, gates, fusion=qi.FUSION_NONE)
+        p32 = qi.Plan(n, qi.F32, gates, fusion=qi.FUSION_GREEDY, max_block_qubits=FUSED_K)
+        s64.set_plus()
+        torch.cuda.synchronize()
+        e0.record(stream)
+        p64.execute(s64)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms64 = e0.elapsed_time(e1)
+        s32.set_plus()
+        torch.cuda.synchronize()
+        e0.record(stream)
+        p32.execute(s32)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms32 = e0.elapsed_time(e1)
+        cmp = s32.compare(s64)
+        en32 = qi.sumop_expectation(s32, terms).real
+        en64 = qi.sumop_expectation(s64, terms).real
+        out.append({"seed": seed, "fused_fp32_ms": ms32, "fp64_per_gate_ms": ms64, "speedup": ms64 / ms32,
+                    "infidelity": cmp["infidelity"], "max_amp_error": cmp["max_abs_err"],
+                    "energy_fp32": en32, "energy_fp64": en64, "energy_error": abs(en32 - en64),
+                    "plan_kernels": p32.stats()["n_kernels"]})
+        del p64, p32
     s64.close()
-    out.update({"fp32_fused_ms_per_step": t32 * 1e3 / steps, "fp64_grouped_ms_per_step": t64_step * 1e3,
-                "speedup_fp32_fused_vs_fp64_grouped": t64_step / (t32 / steps),
-                "term_exponentials_per_s_fp32": len(terms) * steps / t32,
-                "energies_fp32_every_%d" % observe_every: [complex(e).real for e in e32],
-                "energy_after_2_steps_fp32_fused": e32_2, "energy_after_2_steps_fp64_grouped": e64_2,
-                "energy_error_fp32_2_steps": abs(e32_2 - e64_2),
-                "note": "FP32 timed region includes the <H> evaluations (every %d steps)" % observe_every})
+    s32.close()
+    return out
+
+
+def per_gate_leg(qi, workloads, stream, n, peak):
+    """One kernel per gate at n qubits (the plain method's kernels) by gate kind and target
+    qubit, FP32 and FP64: CUDA-event time per launch (qi_plan_profile), achieved bandwidth on
+    the full-pass convention (16 / 32 B per amplitude) and on the bytes the kernel must move
+    (diagonal gates and CNOTs touch half of the amplitudes, a controlled phase a quarter)."""
+    gl = workloads.GateList()
+    cases = []
+    for q in (0, 1, 3, 5, 8, 16, n - 1):
+        gl.add("H", [q]); cases.append(("H (pair)", q, 1.0))
+        gl.add("RY", [q], [], [0.3]); cases.append(("RY (real pair)", q, 1.0))
+        gl.add("RX", [q], [], [0.3]); cases.append(("RX (general pair)", q, 1.0))
+        gl.add("RZ", [q], [], [0.3]); cases.append(("RZ (diagonal)", q, 1.0))
+        gl.add("T", [q]); cases.append(("T (phase on |1>)", q, 0.5))
+    for q in (0, 4, 16, n - 2):
+        gl.add("CNOT", [q + 1], [q]); cases.append(("CNOT", q, 0.5))
+        gl.add("P", [q + 1], [q], [0.3]); cases.append(("controlled phase", q, 0.25))
+        gl.add("SWAP", [q, q + 1]); cases.append(("SWAP", q, 0.5))
+    gates = gl.array()
+    out = {}
+    for label, prec, amp in (("fp32", qi.F32, 8), ("fp64", qi.F64, 16)):
+        plan = qi.Plan(n, prec, gates, fusion=qi.FUSION_NONE)
+        st = qi.DeviceState(n, prec)
+        st.set_stream(stream.cuda_stream)
+        st.set_plus()
+        qi.plan_profile(plan, st)   # warm-up
+        ops, ms = qi.plan_profile(plan, st)
+        rows = []
+        for (kind, q, frac), t in zip(cases, ms):
+            full = (1 << n) * amp * 2
+            rows.append({"gate": kind, "qubit": q, "ms": t, "full_pass_gbs": full / (t / 1e3) / 1e9,
+                         "full_pass_frac": full / (t / 1e3) / 1e9 / peak,
+                         "touched_gbs": frac * full / (t / 1e3) / 1e9,
+                         "touched_frac": frac * full / (t / 1e3) / 1e9 / peak})
+        out[label] = rows
+        st.close()
     return out
 
 
 def run_reference(args):
+    """The reference implementation's CPU path (the oracle port of its rayon data flow; the
+    crate itself needs a Rust toolchain, absent on both machines) on this workload.  A step
+    is one gate of the circuit, timed on its own, cycling over the gate classes; `value`
+    is the whole circuit's layers/s estimated from the per-class mean times, and
+    ms_per_step is the mean time of the timed gates.  No engine code is loaded."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    sys.path.insert(0, ROOT)
     import __graft_entry__ as ge
     ge.build_oracle()
-    ge.load_package()
-    from quant_iron_gb300 import workloads
+    workloads = load_workloads()
+    from _qi_workloads_only._types import GATE_KINDS
     n = args.qubits
     gates = workloads.random_circuit(n, LAYERS, seed=SEED)
     threads = os.cpu_count() or 1
-    need_gb = (1 << n) * 60 / 1e9
     nn = n
-    while nn > 20 and host_mem_gb() < need_gb * 1.3:
+    while nn > 20 and host_mem_gb() < (1 << nn) * 60 / 1e9 * 1.3:
         nn -= 1
-        need_gb = (1 << nn) * 60 / 1e9
     g = gates if nn == n else workloads.random_circuit(nn, LAYERS, seed=SEED)
-    per_step_gates = 2
-    for _ in range(args.warmup):
-        cpu_port_sample(nn, g, 1, threads)
-    times = []
-    for s in range(args.steps):
-        off = (s * per_step_gates) % (len(g) - per_step_gates)
-        times.append(cpu_port_sample(nn, g[off:], per_step_gates, threads))
-    per_gate = statistics.mean(times) * (1 << (n - nn))
-    step_s = per_gate * len(gates)
-    value = LAYERS / step_s
-    sample = ("oracle port of the reference rayon data flow on %d host threads: %d gates of the %d-qubit circuit per "
-              "step, extrapolated to all %d gates%s" % (threads, per_step_gates, nn, len(gates),
-                                                       "" if nn == n else " and scaled by 2^%d" % (n - nn)))
+    est, secs, per_class, desc = reference_cpu_sample(nn, g, GATE_KINDS, args.warmup, args.steps, threads)
+    est *= float(1 << (n - nn))
+    if nn != n:
+        desc += "; scaled by 2^%d amplitudes to %d qubits" % (n - nn, n)
+    value = LAYERS / est
+    world = int(os.environ.get("WORLD_SIZE", "1"))
     line = {"impl": "reference", "metric": "layers/s", "value": value, "unit": "layers/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_s * 1e3, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic",
-            "config": {"workload": "random circuit, %d qubits, %d layers + QFT (%d gates), seed %d" %
-                                   (n, LAYERS, len(gates), SEED), "qubits": n, "layers": LAYERS},
-            "cpu_baseline": {"value": value, "unit": "layers/s", "cores": threads, "kind": "port", "sample": sample},
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(secs) / max(1, len(secs)),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic",
+            "config": workload_config(n, gates, world),
+            "step": "one gate of the circuit on the reference CPU data flow (stratified over gate classes)",
+            "estimated_seconds_per_circuit": est, "classes": per_class,
+            "cpu_baseline": {"value": value, "unit": "layers/s", "cores": threads, "kind": "port", "sample": desc},
             "e2e": {"value": value, "unit": "layers/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
@@ -451,12 +645,18 @@ def main():
                             for k, v in by_kernel.items()}}
     if dom == "k_fused_tc":
         # the same kernel against the tensor roof: 3 split products x 8 * 2^k flop per amplitude
-        # (k = 6: 1536 flop/amp) per launch; peak = the nominal dense TF32 rate (no measured TF32
-        # figure exists for this pool), so the fraction is of nominal
+        # (k = 6: 1536 flop/amp) per launch; peak = the dense tcgen05 kind::tf32 rate measured
+        # here by the engine's own probe kernel (MEASURED_PEAKS.json holds no TF32 figure)
+        probe_clk = ClockSampler(local)
+        probe_clk.start()
+        tf32_peak, probe_ms = qi.tf32_rate_probe(iters=16384, reps=5)
+        pclk = probe_clk.stop()
         tflop = 3 * 8 * (1 << FUSED_K) * (1 << n) / 1e12
-        roofline["tensor"] = {"achieved": tflop / (avg_ms / 1e3), "peak": 1100.0, "unit": "TFLOP/s",
-                              "frac": tflop / (avg_ms / 1e3) / 1100.0, "peak_source": "nominal dense TF32",
-                              "flop_per_amp": 3 * 8 * (1 << FUSED_K)}
+        roofline["tensor"] = {"achieved": tflop / (avg_ms / 1e3), "peak": tf32_peak, "unit": "TFLOP/s",
+                              "frac": tflop / (avg_ms / 1e3) / tf32_peak,
+                              "peak_source": "measured here: qi_tf32_rate_probe (tcgen05.mma kind::tf32 M128 N256 "
+                                             "K8, one CTA per SM, best of 5 launches of %.2f ms)" % probe_ms,
+                              "peak_clocks": pclk, "flop_per_amp": 3 * 8 * (1 << FUSED_K)}
 
     # energy of the final state (FP64 reduction), and the time of SumOp::expectation_value
     energy = qi.sumop_expectation(st, terms).real
@@ -473,49 +673,32 @@ def main():
 
     extra = {}
     if rank == 0 and not args.skip_baselines:
-        # plain FP64 per-gate CUDA path (the denominator of the >= 8x target) and FP32 per-gate
-        plan64 = qi.Plan(n, qi.F64, gates, fusion=qi.FUSION_NONE)
-        s64 = qi.DeviceState(n, qi.F64)
-        s64.set_stream(stream.cuda_stream)
-        s64.set_plus()
-        torch.cuda.synchronize()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        plan64.execute(s64)
-        e1.record(stream)
-        torch.cuda.synchronize()
-        ms64 = e0.elapsed_time(e1)
-        energy64 = qi.sumop_expectation(s64, terms).real
-        # infidelity of the fused FP32 result against the FP64 per-gate result
-        st.set_plus()
-        plan.execute(st)
-        tmp = qi.DeviceState(n, qi.F32)
-        tmp.set_stream(stream.cuda_stream)
-        tmp.copy_from(s64)
-        ov = tmp.inner_product(st)
-        infid = 1.0 - abs(ov) ** 2 / (tmp.norm_sqr() * st.norm_sqr())
-        # max amplitude error on a sampled stride of amplitudes
-        idx = np.linspace(0, (1 << n) - 1, 4096).astype(np.int64)
-        max_err = max(abs(st.amplitude(int(i)) - s64.amplitude(int(i))) for i in idx[:256])
-        tmp.close()
-        s64.close()
-        del plan64
+        # the benchmark family on 5 seeds: fused FP32 against the plain FP64 per-gate path
+        # (the >= 8x target's denominator), full-state errors; seed 0 is the headline circuit
+        seeds = seeds_leg(qi, workloads, stream, torch, n, list(range(5)), terms)
+        s0 = seeds[0]
         plan32 = qi.Plan(n, qi.F32, gates, fusion=qi.FUSION_NONE)
         st.set_plus()
         torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
         plan32.execute(st)
         e1.record(stream)
         torch.cuda.synchronize()
         ms32 = e0.elapsed_time(e1)
         del plan32
-        extra = {"fp64_per_gate_ms": ms64, "fp32_per_gate_ms": ms32, "fused_fp32_ms": ms_per_step,
-                 "speedup_fused_vs_fp64_per_gate": ms64 / ms_per_step,
-                 "infidelity_fused_vs_fp64": infid, "max_amp_error_sampled": max_err,
-                 "energy_fused_fp32": energy, "energy_fp64_per_gate": energy64,
-                 "energy_error": abs(energy - energy64),
-                 "gates_per_s_fused": len(gates) / (ms_per_step / 1e3)}
-        extra["adjoint"] = adjoint_leg(qi, workloads, stream, torch, np)
+        extra = {"fp64_per_gate_ms": s0["fp64_per_gate_ms"], "fp32_per_gate_ms": ms32, "fused_fp32_ms": ms_per_step,
+                 "speedup_fused_vs_fp64_per_gate": s0["fp64_per_gate_ms"] / ms_per_step,
+                 "infidelity_fused_vs_fp64": s0["infidelity"], "max_amp_error_full_state": s0["max_amp_error"],
+                 "energy_fused_fp32": s0["energy_fp32"], "energy_fp64_per_gate": s0["energy_fp64"],
+                 "energy_error": s0["energy_error"], "gates_per_s_fused": len(gates) / (ms_per_step / 1e3),
+                 "seeds": seeds,
+                 "worst_over_seeds": {"infidelity": max(x["infidelity"] for x in seeds),
+                                      "max_amp_error": max(x["max_amp_error"] for x in seeds),
+                                      "energy_error": max(x["energy_error"] for x in seeds),
+                                      "speedup": min(x["speedup"] for x in seeds)}}
+        extra["per_gate"] = per_gate_leg(qi, workloads, stream, n, peak)
+        extra["adjoint"] = adjoint_leg(qi, workloads, stream, torch, np, fd=args.adjoint_fd)
         extra["trotter"] = trotter_leg(qi, workloads, stream, torch, np)
     extra["expectation"] = expectation
 
@@ -546,12 +729,19 @@ def main():
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(stream)
         if pipelined:
+            # circuits one after the other (each state waits for the other's circuit, not for its
+            # download), so each runs at the full device rate while the other state's download and
+            # next upload use the copy engines
             e2e_steps = max(2, args.steps)
             for k in range(e2e_steps):
-                s2 = states[k % 2]
+                s2, other = states[k % 2], states[(k + 1) % 2]
                 s2.upload_async(host_in.data_ptr(), dim)
+                if k > 0:
+                    s2.wait_for(other)   # other's stream so far ends with its circuit
                 plan.execute(s2)
-                s2.download_async(host_out[k % 2].data_ptr(), dim)
+                if k > 0:
+                    other.download_async(host_out[(k - 1) % 2].data_ptr(), dim)
+            states[(e2e_steps - 1) % 2].download_async(host_out[(e2e_steps - 1) % 2].data_ptr(), dim)
             joined = torch.cuda.Event()
             joined.record(stream2)
             stream.wait_event(joined)
@@ -567,8 +757,9 @@ def main():
         e2e_ms = e0.elapsed_time(e1)
         e2e = {"value": LAYERS * e2e_steps / (e2e_ms / 1e3), "unit": "layers/s", "h2d_bytes_per_step": 16 * dim,
                "d2h_bytes_per_step": 16 * dim, "wall_s": wall, "steps": e2e_steps,
-               "pipeline": ("two device states; each step's H2D and D2H on the copy engine overlap the other "
-                            "state's circuit" if pipelined else "one state, transfers in order")}
+               "pipeline": ("two device states, circuits in turn (qi_state_wait); each state's H2D and D2H on the "
+                            "copy engines overlap the other state's circuit" if pipelined
+                            else "one state, transfers in order")}
         if pipelined:
             st2.close()
             del host_out
@@ -577,18 +768,16 @@ def main():
     cpu = None
     if rank == 0 and world == 1 and not args.skip_baselines:
         st.close()
-        cpu = cpu_baseline(n, gates)
+        cpu = cpu_baseline(n, gates, qi._abi.GATE_KINDS)
 
     if rank == 0:
         line = {"metric": "layers/s", "value": value, "unit": "layers/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "c64", "data": "synthetic",
-                "config": {"workload": "random circuit, %d qubits, %d layers + QFT (%d gates), |+>^%d, seed %d; "
-                                       "fused complex-FP32 blocks k<=%d" % (n, LAYERS, len(gates), n, SEED, FUSED_K),
-                           "qubits": n, "layers": LAYERS, "gates": len(gates), "fusion": "greedy k<=%d" % FUSED_K,
-                           "plan": stats, "plan_build_s": plan_s,
-                           "l2": "inputs (%d GiB state) larger than the 129 MB L2; no flush" % ((1 << n) * 8 >> 30),
-                           "parallelism": "replicas" if world > 1 else "single GPU"},
+                "config": workload_config(n, gates, world),
+                "method": {"precision": "complex FP32 state, FP64 reductions", "fusion": "greedy k<=%d" % FUSED_K,
+                           "tensor_cores": "3xTF32 tcgen05 for blocks of k >= 5", "plan": stats,
+                           "plan_build_s": plan_s},
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk, "gpu_launches": launches}
         line.update(extra)
         print(json.dumps(line))

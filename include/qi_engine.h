@@ -3,9 +3,8 @@
  *
  * This is the drop-in boundary.  Every entry point takes plain pointers and
  * sizes and returns a qi_status.  The Rust side of quant-iron binds these in an
- * `extern "C"` block (the binding is shown in INTEGRATION.md); each function
- * names the reference item it replaces as `file:line` within the quant-iron
- * crate (src/...).
+ * `extern "C"` block next to its build.rs; each function names the reference
+ * item it replaces as `file:line` within the quant-iron crate (src/...).
  *
  * Conventions shared by all calls
  *  - Amplitude index bit q is qubit q (little-endian), as in
@@ -119,6 +118,13 @@ qi_status qi_state_download(qi_state *s, double *amps, uint64_t num_amps);
  * while the other computes.  A pageable host buffer returns InvalidInputValue. */
 qi_status qi_state_upload_async(qi_state *s, const double *amps, uint64_t num_amps);
 qi_status qi_state_download_async(qi_state *s, double *amps, uint64_t num_amps);
+/* Order the work issued on s after this call behind the work issued so far on
+ * other's stream (a CUDA event; no host synchronisation).  With two states in
+ * flight, a caller puts each state's circuit behind the other's: the circuits
+ * then run one after the other at full device rate while the idle state's
+ * transfers proceed on the copy engines, instead of both circuits sharing the
+ * SMs and finishing together with every transfer left to wait. */
+qi_status qi_state_wait(qi_state *s, qi_state *other);
 
 /* Device-side constructors: State::new_zero / new_basis_n / new_plus /
  * new_minus / new_ghz (state.rs:165-325), filled in place. */
@@ -138,6 +144,11 @@ qi_status qi_state_copy(qi_state *dst, const qi_state *src);
  * `State + State` / `State - State` (state.rs:2773-2862) as y += a*x. */
 qi_status qi_state_scale(qi_state *s, double re, double im);
 qi_status qi_state_axpy(qi_state *y, double re, double im, const qi_state *x);
+/* Comparison of two states of the same size and any precisions (FP64
+ * arithmetic): out[0] = max_i |a_i - b_i|, out[1] = sum_i |a_i - b_i|^2,
+ * out[2..3] = <b|a>.  No counterpart in the reference; it measures the
+ * max-amplitude error and infidelity of an FP32 state against an FP64 one. */
+qi_status qi_state_compare(qi_state *a, qi_state *b, double out[4]);
 /* Reductions, accumulated in FP64 on the device:
  * inner_product <a|b> = sum conj(a_i) b_i (state.rs:890-917); norm^2. */
 qi_status qi_state_inner_product(qi_state *a, qi_state *b, double out[2]);
@@ -177,7 +188,15 @@ enum qi_gate_kind {
     /* Circuit-only gate variants (src/components/gate.rs:13-52). */
     QI_GATE_PAULI_STRING    = 20, /* Gate::PauliString -> apply_normalised (gate.rs:115-117) */
     QI_GATE_PAULI_EVOLUTION = 21, /* Gate::PauliTimeEvolution -> apply_exp_neg_i_dt (gate.rs:118-120); params[2] = dt */
-    QI_GATE_KIND_COUNT      = 22
+    /* Gate::Measurement(basis, indices) -> State::measure, keeping the collapsed state
+     * (gate.rs:19, :104-106; state.rs:525-730).  n_targets = 0; targets[0] = basis
+     * (QI_BASIS_*); the measured qubits, in outcome-bit order, in controls[0 .. n_controls)
+     * (n_controls = 0: every qubit, as State::measure with no indices); params[0..7] = the
+     * custom basis matrix for QI_BASIS_CUSTOM; xmask = seed of the outcome draw (the
+     * reference draws from the unseeded rand::rng(), state.rs:601).  At most 24 measured
+     * qubits.  A plan runs it between its fused segments (nothing is fused across it). */
+    QI_GATE_MEASUREMENT     = 22,
+    QI_GATE_KIND_COUNT      = 23
 };
 
 #define QI_MAX_CONTROLS 32
@@ -245,12 +264,15 @@ qi_status qi_sumop_expectation(qi_state *s, const qi_pauli_term *terms, int64_t 
  * the device-wide synchronisation of an allocation.  All temporaries live in
  * one static device array of 137,472 bytes that every GPU loading this
  * library holds until exit.  Limits: n_terms <= 4096, and at most 2048 terms
- * sharing one X mask (else InvalidInputValue).  The first call on a device
- * looks up that array's device address (cudaGetSymbolAddress) with the device
- * current; make that first call before any stream capture.  All calls share
- * the array: calls whose work overlaps on the GPU (other streams, other host
- * threads) race.  Work is issued on `cuda_stream` (NULL = legacy default
- * stream) and the call returns after it completes. */
+ * sharing one X mask (else InvalidInputValue).  `amps` and `cuda_stream`
+ * must belong to the current device (else InvalidInputValue).  The first call
+ * on a device looks up that array's device address (cudaGetSymbolAddress) and
+ * sets the group kernels' shared-memory limit, with the device current; make
+ * that first call before any stream capture.  The address is kept for the
+ * life of the process, so a cudaDeviceReset between calls is not supported.
+ * All calls share the array: calls whose work overlaps on the GPU (other
+ * streams, other host threads) race.  Work is issued on `cuda_stream` (NULL =
+ * legacy default stream) and the call returns after it completes. */
 qi_status qi_sumop_expectation_noalloc(const void *amps, int32_t num_qubits, int32_t precision,
                                        const qi_pauli_term *terms, int64_t n_terms, void *cuda_stream,
                                        double out[2]);
@@ -360,6 +382,13 @@ qi_status qi_measure(qi_state *s, int32_t basis, const double *custom_u, const i
 qi_status qi_measure_n(qi_state *s, int32_t basis, const double *custom_u, const int32_t *qubits, int32_t n_qubits,
                        int64_t n_shots, uint64_t seed, uint64_t *outcomes_out);
 
+/* Dense tcgen05.mma kind::tf32 rate of the current GPU (no reference
+ * counterpart): one CTA per SM issues `iters` M128 x N256 x K8 products from
+ * tensor-memory and shared-memory operands into one accumulator, no global
+ * memory traffic; best of `reps` timed launches (CUDA events) after one
+ * warm-up.  The tensor roof the 3xTF32 fused blocks are measured against. */
+qi_status qi_tf32_rate_probe(int32_t iters, int32_t reps, double *tflops_out, double *ms_out);
+
 /* ------------------------------------------------------------------------ */
 /* Learned fusion cost model (no reference counterpart)                      */
 /* ------------------------------------------------------------------------ */
@@ -393,9 +422,11 @@ typedef struct qi_plan_op_info {
                                5 Pauli exponential, 6 Pauli string + normalise, 7 diagonal block,
                                8 renormalisation, 9 phase polynomial (a run of diagonal blocks),
                                10 grouped Pauli exponentials (a run with X-masks in {0, X}),
-                               11 qubit permutation (a run of SWAP / X gates; qi_plan_op_bitperm) */
+                               11 qubit permutation (a run of SWAP / X gates; qi_plan_op_bitperm),
+                               12 measurement (basis in zmask, seed in xmask) */
     int32_t  k;             /* number of targets (kind 9: number of diagonal blocks in the run;
-                               kind 10: number of exponentials in the run; kind 11: gates in the run) */
+                               kind 10: number of exponentials in the run; kind 11: gates in the run;
+                               kind 12: measured qubits, the first six in targets) */
     int32_t  targets[6];    /* sorted ascending for kinds 3, 4, 7 */
     int32_t  tensor_cores;  /* kind 4: 1 if the block runs on the tcgen05 tensor-core kernel */
     int32_t  phase_poly;    /* kind 4: 1 if a phase polynomial (qi_plan_op_phase_poly) follows the block

@@ -41,6 +41,7 @@ _sig = {
     "oracle_measure": (_i32, [_vp, _i32, _vp, _i32, _d, ctypes.POINTER(_i64), _vp]),
     "oracle_unitary2_check": (_i32, [_pd]),
     "oracle_port_execute": (_d, [_vp, _i32, _vp, _i64, _i32]),
+    "oracle_port_execute_timed": (_d, [_vp, _i32, _vp, _i64, _i32, _pd]),
 }
 for _n, (_r, _a) in _sig.items():
     f = getattr(lib, _n)
@@ -177,4 +178,15 @@ def port_execute(state, n, gates, threads):
     s = _vec(state)
     g = np.ascontiguousarray(gates)
     secs = lib.oracle_port_execute(s.ctypes.data, n, g.ctypes.data, g.size, int(threads))
+    return s, secs
+
+
+def port_execute_timed(state, n, gates, threads):
+    """port_execute with one wall time per gate; returns (state, seconds per gate).
+    A C-contiguous complex128 `state` is updated in place (no copy)."""
+    s = np.ascontiguousarray(state, dtype=np.complex128)
+    g = np.ascontiguousarray(gates)
+    secs = np.zeros(g.size, dtype=np.float64)
+    lib.oracle_port_execute_timed(s.ctypes.data, n, g.ctypes.data, g.size, int(threads),
+                                  secs.ctypes.data_as(_pd))
     return s, secs

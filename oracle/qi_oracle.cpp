@@ -393,7 +393,69 @@ static qi_gate resolve(const qi_gate &g, const double *theta) {
     return r;
 }
 
+int oracle_measure(double *sv, int n, const int32_t *qubits, int nq, double r, int64_t *outcome,
+                   double *probs_out);
+
+// SplitMix64 (Steele, Lea, Flood 2014), the seeded stand-in for the reference's unseeded
+// rand::rng() in State::measure (state.rs:601): r = top 53 bits / 2^53.
+static double uniform01(uint64_t x) {
+    x += 0x9E3779B97F4A7C15ull;
+    x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+    x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+    x ^= x >> 31;
+    return (double)(x >> 11) * 0x1.0p-53;
+}
+
+// Gate::Measurement (gate.rs:104-106) -> State::measure (state.rs:525-730), keeping the new
+// state: basis change on every measured qubit (X: H; Y: S-dagger then H; Custom: U), the
+// computational measurement with r drawn from the gate's seed (xmask), then the change back
+// (X: H; Y: H then S; Custom: U-dagger, calculate_adjoint state.rs:17-22).
+static Err apply_measurement(C *s, int n, const qi_gate &g) {
+    const int basis = g.targets[0];
+    if (g.n_targets != 0) return {QI_ERR_INVALID_NUMBER_OF_QUBITS, g.n_targets, -1};
+    if (basis < QI_BASIS_COMPUTATIONAL || basis > QI_BASIS_CUSTOM) return {QI_ERR_INVALID_INPUT_VALUE, basis, -1};
+    std::vector<int32_t> q(g.controls, g.controls + g.n_controls);
+    if (q.empty()) for (int k = 0; k < n; ++k) q.push_back(k);
+    if ((int)q.size() > n) return {QI_ERR_INVALID_NUMBER_OF_QUBITS, n, -1};
+    for (int32_t x : q)
+        if (x < 0 || x >= n) return {QI_ERR_INVALID_QUBIT_INDEX, x, n};
+    auto each = [&](int kind, const double *m8) {
+        for (int32_t x : q) {
+            qi_gate h;
+            std::memset(&h, 0, sizeof(h));
+            h.kind = kind;
+            h.n_targets = 1;
+            h.targets[0] = x;
+            h.param_ids[0] = h.param_ids[1] = h.param_ids[2] = -1;
+            if (m8) std::memcpy(h.params, m8, 8 * sizeof(double));
+            Err e = apply_gate(s, n, h);
+            if (e.code) return e;
+        }
+        return ok();
+    };
+    const double *u = g.params;
+    const double ud[8] = {u[0], -u[1], u[4], -u[5], u[2], -u[3], u[6], -u[7]};
+    Err e = ok();
+    if (basis == QI_BASIS_X) e = each(QI_GATE_H, nullptr);
+    else if (basis == QI_BASIS_Y) {
+        e = each(QI_GATE_SDAG, nullptr);
+        if (!e.code) e = each(QI_GATE_H, nullptr);
+    } else if (basis == QI_BASIS_CUSTOM) e = each(QI_GATE_U2, u);
+    if (e.code) return e;
+    int64_t outcome = 0;
+    if (oracle_measure(reinterpret_cast<double *>(s), n, q.data(), (int)q.size(), uniform01(g.xmask), &outcome,
+                       nullptr))
+        return g_last;
+    if (basis == QI_BASIS_X) e = each(QI_GATE_H, nullptr);
+    else if (basis == QI_BASIS_Y) {
+        e = each(QI_GATE_H, nullptr);
+        if (!e.code) e = each(QI_GATE_S, nullptr);
+    } else if (basis == QI_BASIS_CUSTOM) e = each(QI_GATE_U2, ud);
+    return e;
+}
+
 static Err apply_any(C *s, int n, const qi_gate &g) {
+    if (g.kind == QI_GATE_MEASUREMENT) return apply_measurement(s, n, g);
     if (g.kind == QI_GATE_PAULI_STRING) {       // gate.rs:115-117 -> apply_normalised
         qi_pauli_term t = {g.params[0], g.params[1], g.xmask, g.zmask};
         Err e = validate_term(n, t);
@@ -695,6 +757,23 @@ double oracle_port_execute(double *sv, int n, const qi_gate *gates, int64_t n_ga
     auto t1 = std::chrono::steady_clock::now();
     std::memcpy(sv, st.data(), dim * sizeof(C));
     return std::chrono::duration<double>(t1 - t0).count();
+}
+
+// As oracle_port_execute, with the wall time of each gate written to secs_out[k].
+double oracle_port_execute_timed(double *sv, int n, const qi_gate *gates, int64_t n_gates, int threads,
+                                 double *secs_out) {
+    const uint64_t dim = 1ull << n;
+    std::vector<C> st(amp(sv), amp(sv) + dim);
+    double total = 0.0;
+    for (int64_t k = 0; k < n_gates; ++k) {
+        auto t0 = std::chrono::steady_clock::now();
+        port_gate(st, n, gates[k], threads);
+        auto t1 = std::chrono::steady_clock::now();
+        secs_out[k] = std::chrono::duration<double>(t1 - t0).count();
+        total += secs_out[k];
+    }
+    std::memcpy(sv, st.data(), dim * sizeof(C));
+    return total;
 }
 
 }  // extern "C"

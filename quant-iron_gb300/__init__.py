@@ -89,6 +89,10 @@ class DeviceState:
         check(lib.qi_state_device_ptr(self.h, ctypes.byref(p)))
         return p.value
 
+    def wait_for(self, other):
+        """Order this state's subsequent work behind the work issued so far on `other`."""
+        check(lib.qi_state_wait(self.h, other.h))
+
     def synchronize(self):
         check(lib.qi_state_synchronize(self.h))
 
@@ -154,6 +158,16 @@ class DeviceState:
         out = (ctypes.c_double * 2)()
         check(lib.qi_state_inner_product(self.h, other.h, out))
         return complex(out[0], out[1])
+
+    def compare(self, reference):
+        """Errors of this state against `reference` (same size, any precisions; FP64 on the
+        device): max amplitude error, squared distance, overlap <reference|self>, infidelity."""
+        out = (ctypes.c_double * 4)()
+        check(lib.qi_state_compare(self.h, reference.h, out))
+        ov = complex(out[2], out[3])
+        na, nb = self.norm_sqr(), reference.norm_sqr()
+        return {"max_abs_err": out[0], "dist_sqr": out[1], "overlap": ov,
+                "infidelity": 1.0 - abs(ov) ** 2 / (na * nb)}
 
     def norm_sqr(self):
         out = ctypes.c_double()
@@ -376,6 +390,14 @@ def _basis_args(basis, custom):
     return b, u
 
 
+def tf32_rate_probe(iters=16384, reps=5):
+    """Dense tcgen05 kind::tf32 rate of the current GPU: (TFLOP/s, ms of the best launch)."""
+    tf = ctypes.c_double()
+    ms = ctypes.c_double()
+    check(lib.qi_tf32_rate_probe(int(iters), int(reps), ctypes.byref(tf), ctypes.byref(ms)))
+    return tf.value, ms.value
+
+
 def splitmix_uniform(seed):
     """The uniform draw qi_measure uses for `seed`: (splitmix64(seed) >> 11) * 2^-53."""
     m = (1 << 64) - 1
@@ -433,7 +455,8 @@ def adjoint_sweep_plan(num_qubits, precision, gates, theta, fusion=FUSION_GREEDY
     return [(int(kinds[i]), int(hi[i]), int(lo[i])) for i in range(count.value)]
 
 
-def adjoint_gradient(state, gates, theta, terms, fusion=FUSION_GREEDY, max_block_qubits=0, use_tensor_cores=0):
+def adjoint_gradient(state, gates, theta, terms, fusion=FUSION_GREEDY, max_block_qubits=0, use_tensor_cores=0,
+                     renorm_every=0):
     """dE/dtheta of E = <psi(theta)|H|psi(theta)> by one forward and one reverse sweep.
     `state` holds |psi0> before and after the call.  Returns (E, grads)."""
     gates = np.ascontiguousarray(gates, dtype=GATE_DTYPE)
@@ -441,7 +464,7 @@ def adjoint_gradient(state, gates, theta, terms, fusion=FUSION_GREEDY, max_block
     h = _terms(terms)
     grads = np.zeros(t.size, dtype=np.float64)
     energy = ctypes.c_double()
-    opts = _options(fusion, max_block_qubits, use_tensor_cores)
+    opts = _options(fusion, max_block_qubits, use_tensor_cores, renorm_every)
     pd = ctypes.POINTER(ctypes.c_double)
     check(lib.qi_adjoint_gradient(state.h, gates.ctypes.data if gates.size else None, gates.size, t.ctypes.data_as(pd),
                                   t.size, h.ctypes.data if h.size else None, h.size, ctypes.byref(opts),

@@ -6,7 +6,8 @@ library is missing the import fails with an error that says how to build it.
 import ctypes
 import os
 
-import numpy as np
+from ._types import (F32, F64, FUSION_GREEDY, FUSION_LEARNED, FUSION_NONE, FUSION_PAULI_GROUPS,  # noqa: F401
+                     GATE_DTYPE, GATE_KINDS, MAX_CONTROLS, OK, STATUS_NAMES, TERM_DTYPE)
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "lib", "libqi_gb300.so")
@@ -15,53 +16,6 @@ if not os.path.exists(LIB_PATH):
     raise ImportError("quant-iron GB300 engine library not found at %s; build it with "
                       "`python -c 'import __graft_entry__ as g; g.build()'`" % LIB_PATH)
 lib = ctypes.CDLL(LIB_PATH)
-
-# ---------------------------------------------------------------- constants
-OK = 0
-F64 = 0
-F32 = 1
-FUSION_NONE = 0
-FUSION_GREEDY = 1
-FUSION_LEARNED = 2
-FUSION_PAULI_GROUPS = 3
-MAX_CONTROLS = 32
-
-# qi_status -> name of the quant_iron::errors::Error variant (src/errors.rs:4-97)
-STATUS_NAMES = {
-    -1: "InvalidNumberOfMeasurements",
-    -2: "OverlappingControlAndTargetQubits",
-    -3: "InvalidNumberOfQubits",
-    -4: "InvalidQubitIndex",
-    -5: "StateVectorNotNormalised",
-    -6: "NonUnitaryMatrix",
-    -7: "InvalidNumberOfInputs",
-    -8: "MismatchedNumberOfParameters",
-    -9: "UnknownError",
-    -10: "OpenCLError",
-    -11: "GpuContextLockError",
-    -12: "CircuitMacroError",
-    -13: "InvalidInputValue",
-    -14: "ZeroNorm",
-    -15: "InvalidPauliStringCoefficient",
-    -16: "OutOfMemory",
-    -17: "Timeout",
-    -18: "NullArgument",
-    -19: "Unsupported",
-}
-
-GATE_KINDS = dict(H=0, X=1, Y=2, Z=3, S=4, T=5, SDAG=6, TDAG=7, P=8, RX=9, RY=10, RZ=11, U2=12, RYPHASE=13,
-                  RYPHASE_DAG=14, CNOT=15, SWAP=16, MATCHGATE=17, TOFFOLI=18, IDENTITY=19, PAULI_STRING=20,
-                  PAULI_EVOLUTION=21)
-
-# qi_gate as a numpy structured dtype (same layout as the C struct)
-GATE_DTYPE = np.dtype([
-    ("kind", "<i4"), ("n_targets", "<i4"), ("n_controls", "<i4"), ("param_ids", "<i4", (3,)),
-    ("targets", "<i4", (2,)), ("controls", "<i4", (MAX_CONTROLS,)), ("params", "<f8", (8,)),
-    ("xmask", "<u8"), ("zmask", "<u8"),
-], align=True)
-assert GATE_DTYPE.itemsize == 240, GATE_DTYPE.itemsize
-
-TERM_DTYPE = np.dtype([("re", "<f8"), ("im", "<f8"), ("xmask", "<u8"), ("zmask", "<u8")])
 
 
 class ErrorInfo(ctypes.Structure):
@@ -106,6 +60,7 @@ SIGNATURES = {
     "qi_state_get_stream": (_i32, [_vp, ctypes.POINTER(_vp)]),
     "qi_state_device_ptr": (_i32, [_vp, ctypes.POINTER(_vp)]),
     "qi_state_synchronize": (_i32, [_vp]),
+    "qi_state_wait": (_i32, [_vp, _vp]),
     "qi_state_upload": (_i32, [_vp, _vp, _u64]),
     "qi_state_download": (_i32, [_vp, _vp, _u64]),
     "qi_state_upload_async": (_i32, [_vp, _vp, _u64]),
@@ -120,6 +75,8 @@ SIGNATURES = {
     "qi_state_scale": (_i32, [_vp, _d, _d]),
     "qi_state_axpy": (_i32, [_vp, _d, _d, _vp]),
     "qi_state_inner_product": (_i32, [_vp, _vp, _pd]),
+    "qi_state_compare": (_i32, [_vp, _vp, _pd]),
+    "qi_tf32_rate_probe": (_i32, [_i32, _i32, _pd, _pd]),
     "qi_state_norm_sqr": (_i32, [_vp, _pd]),
     "qi_state_normalise": (_i32, [_vp]),
     "qi_state_tensor_product": (_i32, [_vp, _vp, _vp]),

@@ -512,6 +512,41 @@ static void fill_adj_positions(AdjParams &p, const GateMatrix &gm, uint64_t cmas
     p.np = np;
 }
 
+// FP32 sweeps: the 2x2 matrix u (row-major complex, FP64) a stage un-applies, replaced by the
+// FP32 values the kernel will use, chosen so that they form an exact multiple r of a unitary;
+// returns r^2.  Entry-wise rounding keeps that form for the real, diagonal and reflection
+// matrices of the gate set; otherwise u is first brought to SU(2) by a global phase (which
+// cancels in <lambda|D|psi>, psi and lambda carrying the same phase) and a, b of
+// [[a, -conj(b)], [b, conj(a)]] are rounded.  Un-applying then scales psi and lambda by
+// exactly r, a deterministic drift of up to ~1e-7 per stage that the host divides out of
+// the gradient instead of letting it accumulate over the sweep.
+static double fp32_stage_matrix(double *u) {
+    double f[8];
+    for (int i = 0; i < 8; ++i) f[i] = (double)(float)u[i];
+    auto dot = [&](int a, int b, double &re, double &im) {   // conj(col a) . col b
+        re = f[2 * a] * f[2 * b] + f[2 * a + 1] * f[2 * b + 1] + f[2 * (a + 2)] * f[2 * (b + 2)] +
+             f[2 * (a + 2) + 1] * f[2 * (b + 2) + 1];
+        im = f[2 * a] * f[2 * b + 1] - f[2 * a + 1] * f[2 * b] + f[2 * (a + 2)] * f[2 * (b + 2) + 1] -
+             f[2 * (a + 2) + 1] * f[2 * (b + 2)];
+    };
+    double c00, i00, c11, i11, c01r, c01i;
+    dot(0, 0, c00, i00);
+    dot(1, 1, c11, i11);
+    dot(0, 1, c01r, c01i);
+    if (c01r == 0.0 && c01i == 0.0 && std::fabs(c00 - c11) <= 1e-15 * c00) {
+        std::copy(f, f + 8, u);
+        return c00;
+    }
+    // det u = e^{i phi}; u e^{-i phi / 2} = [[a, -conj(b)], [b, conj(a)]]
+    const std::complex<double> u00(u[0], u[1]), u01(u[2], u[3]), u10(u[4], u[5]), u11(u[6], u[7]);
+    const std::complex<double> ph = std::exp(std::complex<double>(0.0, -0.5 * std::arg(u00 * u11 - u01 * u10)));
+    const std::complex<double> a = u00 * ph, b = u10 * ph;
+    const double ar = (float)a.real(), ai = (float)a.imag(), br = (float)b.real(), bi = (float)b.imag();
+    u[0] = ar; u[1] = ai; u[2] = -br; u[3] = bi;
+    u[4] = br; u[5] = bi; u[6] = ar; u[7] = -ai;
+    return ar * ar + ai * ai + br * br + bi * bi;
+}
+
 }  // namespace qi
 
 using namespace qi;
@@ -534,6 +569,8 @@ static Status resolve_adjoint_gates(int n, const qi_gate *gates, int64_t n_gates
         }
         if (g.kind == QI_GATE_PAULI_STRING)
             return err(QI_ERR_UNSUPPORTED, j, -1, "a normalising Pauli-string gate has no inverse");
+        if (g.kind == QI_GATE_MEASUREMENT)
+            return err(QI_ERR_UNSUPPORTED, j, -1, "a measurement has no inverse");
         Status st = gate_to_matrix(n, g, &mats[(size_t)j]);
         if (!st.ok()) return st;
         resolved[(size_t)j] = g;
@@ -652,9 +689,37 @@ extern "C" qi_status qi_adjoint_gradient(qi_state *s, const qi_gate *gates, int6
         Status st = resolve_adjoint_gates(n, gates, n_gates, theta, n_theta, resolved, mats);
         if (!st.ok()) return publish(st);
     }
-    // forward sweep; the reverse sweep's fixed-gate segments use the same options
+    // forward sweep; the reverse sweep's fixed-gate segments use the same options.  FP32 states
+    // fuse at most 5 qubits per block unless the caller chose: a 6-qubit tensor-core block sums
+    // 48 truncating FP32 steps per amplitude (a 5-qubit one 24), and at 26 qubits that drift
+    // alone took the gradient from 7e-7 to 1.3e-6 of the FP64 result.
     qi_exec_options plan_opts = {QI_FUSION_GREEDY, 0, 0, 0};
     if (forward_opts) plan_opts = *forward_opts;
+    if (s->prec == QI_F32 && plan_opts.max_block_qubits <= 0) plan_opts.max_block_qubits = 5;
+    // psi_0 stays untouched in the caller's buffer: the sweep runs on a copy (un-applying psi in
+    // FP32 would hand back psi_0 with the sweep's rounding in it); without room for the copy it
+    // runs in place and psi_0 is restored by the sweep itself.
+    void *const psi_home = s->amps;
+    void *work = nullptr;
+    if (cudaMalloc(&work, s->bytes()) == cudaSuccess) {
+        e = cudaMemcpyAsync(work, psi_home, s->bytes(), cudaMemcpyDeviceToDevice, s->stream);
+        if (e != cudaSuccess) {
+            cudaFree(work);
+            return publish(cuda_status(e, "copy psi_0"));
+        }
+        s->amps = work;
+    } else {
+        work = nullptr;
+        cudaGetLastError();
+    }
+    auto bail = [&](Status st) {   // before lambda exists: psi is in `work` (or in place)
+        if (work) {
+            cudaStreamSynchronize(s->stream);
+            cudaFree(s->amps);
+            s->amps = psi_home;
+        }
+        return publish(st);
+    };
     {
         qi_plan plan;
         plan.n = n;
@@ -667,18 +732,18 @@ extern "C" qi_status qi_adjoint_gradient(qi_state *s, const qi_gate *gates, int6
         if (st.ok()) st = plan_execute(&plan, s);
         if (plan.d_mats) cudaFree(plan.d_mats);
         if (plan.d_tc) cudaFree(plan.d_tc);
-        if (!st.ok()) return publish(st);
+        if (!st.ok()) return bail(st);
     }
     double ev[2] = {0, 0};
     if (n_terms > 0) {
         Status st = sumop_expectation(s, terms, n_terms, ev);
-        if (!st.ok()) return publish(st);
+        if (!st.ok()) return bail(st);
     }
     if (energy_out) *energy_out = ev[0];
     // lambda = H psi
     qi_state *lam = nullptr;
     qi_status cs = qi_state_create(n, s->prec, &lam);
-    if (cs != QI_OK) return cs;
+    if (cs != QI_OK) return bail(err(cs, -1, -1, "lambda state"));
     qi_state_set_stream(lam, s->stream);
     Status st = ok_status();
     if (n_terms > 0) st = sumop_apply(lam, s, terms, n_terms);
@@ -690,12 +755,24 @@ extern "C" qi_status qi_adjoint_gradient(qi_state *s, const qi_gate *gates, int6
         e = cudaMalloc(&d_gres, (size_t)nslots * sizeof(double));
         if (e != cudaSuccess) st = cuda_status(e, "cudaMalloc(gradient slots)");
     }
-    std::vector<std::pair<int64_t, int32_t>> slot_param;   // slot -> parameter id
+    struct SlotParam {
+        int64_t slot;
+        int32_t param;
+        double factor;   // divides out the norm drift psi and lambda carried when the term was taken
+    };
+    std::vector<SlotParam> slot_param;
     int64_t slot = nslots;
     const bool f32 = s->prec == QI_F32;
     std::vector<std::unique_ptr<qi_plan>> seg_plans;   // kept until the sweep has run
-    void *const psi_home = s->amps;   // psi's own buffer: holds psi again before returning
     void *scratch = nullptr;          // third state buffer for affine gathers (rotates with psi, lambda)
+    // Norm^2 of psi and lambda relative to where the sweep started (FP32 sweeps): exact stage
+    // scales (fp32_stage_matrix) multiply in; after a tensor-core plan segment (which rounds
+    // toward zero) both are measured.  A derivative term is divided by sqrt(cpsi * clam).
+    double cpsi = 1.0, clam = 1.0, npsi0 = 1.0, nlam0 = 1.0;
+    if (st.ok() && f32) st = state_reduce_norm_sqr(s, &npsi0);
+    if (st.ok() && f32 && n_terms > 0) st = state_reduce_norm_sqr(lam, &nlam0);
+    if (!(npsi0 > 0.0)) npsi0 = 1.0;
+    if (!(nlam0 > 0.0)) nlam0 = 1.0;
     const std::vector<SweepStep> steps = plan_reverse_sweep(mats, resolved, f32, plan_opts.fusion);
     for (size_t si = 0; si < steps.size() && st.ok(); ++si) {
         const int64_t j = steps[si].hi, jj = steps[si].lo;
@@ -726,6 +803,9 @@ extern "C" qi_status qi_adjoint_gradient(qi_state *s, const qi_gate *gates, int6
                 }
             int used[64] = {0};
             std::vector<std::pair<int, int32_t>> comp_param;   // component -> parameter id
+            double r2[kMultiQubits][kMultiStages];
+            for (int i = 0; i < kMultiQubits; ++i)
+                for (int t = 0; t < kMultiStages; ++t) r2[i][t] = 1.0;
             for (int64_t k = j; k > jj && st.ok(); --k) {
                 const GateMatrix &gm = mats[(size_t)k];
                 const qi_gate &g = resolved[(size_t)k];
@@ -753,6 +833,7 @@ extern "C" qi_status qi_adjoint_gradient(qi_state *s, const qi_gate *gates, int6
                         dd[2 * (2 * r + c)] = re;
                         dd[2 * (2 * r + c) + 1] = im;
                     }
+                if (f32) r2[b][t] = fp32_stage_matrix(ui);
                 bool diag = true, real = true;
                 for (int e = 0; e < 8; ++e) {
                     const bool off = e == 2 || e == 3 || e == 4 || e == 5;
@@ -780,7 +861,16 @@ extern "C" qi_status qi_adjoint_gradient(qi_state *s, const qi_gate *gates, int6
             k_finalize_to<<<1, 256, 0, s->stream>>>(s->d_partials, (int)nb, M * S, kMultiComps, d_gres + slot);
             count_launch(2);
             st = check_launch("k_finalize_to");
-            for (auto &cp : comp_param) slot_param.push_back({slot + cp.first, cp.second});
+            // the kernel runs qubit by qubit (mp.pos order), each qubit's stages in order: a
+            // stage's term sees every scale applied before it in that order
+            double fac[kMultiComps];
+            for (int i = 0; i < M; ++i)
+                for (int t = 0; t < S; ++t) {
+                    fac[i * S + t] = 1.0 / std::sqrt(cpsi * clam);
+                    cpsi *= r2[i][t];
+                    clam *= r2[i][t];
+                }
+            for (auto &cp : comp_param) slot_param.push_back({slot + cp.first, cp.second, fac[cp.first]});
             continue;
         }
         bool as_plan = kind == kSweepPlan;
@@ -828,6 +918,15 @@ extern "C" qi_status qi_adjoint_gradient(qi_state *s, const qi_gate *gates, int6
             if (st.ok()) st = upload_plan(seg.get());
             if (st.ok()) st = plan_execute(seg.get(), s);
             if (st.ok()) st = plan_execute(seg.get(), lam);
+            if (st.ok() && f32 && !seg->tc.empty()) {   // tensor-core blocks: measure the drift
+                double a = 0.0, b = 0.0;
+                st = state_reduce_norm_sqr(s, &a);
+                if (st.ok()) st = state_reduce_norm_sqr(lam, &b);
+                if (st.ok()) {
+                    cpsi = a / npsi0;
+                    if (n_terms > 0) clam = b / nlam0;
+                }
+            }
             seg_plans.push_back(std::move(seg));
             continue;
         }
@@ -866,6 +965,12 @@ extern "C" qi_status qi_adjoint_gradient(qi_state *s, const qi_gate *gates, int6
         p.nd = nd;
         for (int q = 0; q < nd && st.ok(); ++q) st = derivative_matrix(n, g, ids[q], p.d[q]);
         if (!st.ok()) break;
+        // an uncontrolled single-qubit stage scales both states by exactly r (FP32); the term
+        // uses psi after the un-apply and lambda before it
+        const double r2g = (f32 && gm.nt == 1 && cm == 0) ? fp32_stage_matrix(p.uinv) : 1.0;
+        const double facg = 1.0 / std::sqrt(cpsi * r2g * clam);
+        cpsi *= r2g;
+        clam *= r2g;
         const int nc = __builtin_popcountll(cm);
         p.nwork = 1ull << (n - gm.nt - nc);
         uint64_t nb64 = (p.nwork + 255) / 256;
@@ -881,7 +986,7 @@ extern "C" qi_status qi_adjoint_gradient(qi_state *s, const qi_gate *gates, int6
         k_finalize_to<<<1, 256, 0, s->stream>>>(s->d_partials, (int)nb, nd, 4, d_gres + slot);
         count_launch(2);
         st = check_launch("k_adjoint");
-        for (int q = 0; q < nd; ++q) slot_param.push_back({slot + q, g.param_ids[ids[q]]});
+        for (int q = 0; q < nd; ++q) slot_param.push_back({slot + q, g.param_ids[ids[q]], facg});
     }
     if (st.ok()) {
         for (int64_t k = 0; k < n_theta; ++k) grads_out[k] = 0.0;
@@ -890,10 +995,13 @@ extern "C" qi_status qi_adjoint_gradient(qi_state *s, const qi_gate *gates, int6
                                             s->stream);
         if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
         if (e != cudaSuccess) st = cuda_status(e, "adjoint");
-        for (auto &sp : slot_param) grads_out[sp.second] += 2.0 * h[(size_t)sp.first];
+        for (auto &sp : slot_param) grads_out[sp.param] += 2.0 * h[(size_t)sp.slot] * sp.factor;
     }
     cudaStreamSynchronize(s->stream);
-    if (s->amps != psi_home) {   // psi_home is lambda's or the scratch buffer now
+    if (work) {   // psi_0 never left the caller's buffer; psi ends in one of the sweep's buffers
+        cudaFree(s->amps);
+        s->amps = psi_home;
+    } else if (s->amps != psi_home) {   // psi_home is lambda's or the scratch buffer now
         e = cudaMemcpyAsync(psi_home, s->amps, s->bytes(), cudaMemcpyDeviceToDevice, s->stream);
         if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
         if (e != cudaSuccess && st.ok()) st = cuda_status(e, "restore psi buffer");

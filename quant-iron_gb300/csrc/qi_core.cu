@@ -187,6 +187,61 @@ __global__ void k_inner_partial(const typename Cx<T>::V2 *a, const typename Cx<T
     }
 }
 
+// Comparison of two states of any precisions (a verification tool, FP64 throughout): per
+// block [max |a_i - b_i|^2, sum |a_i - b_i|^2, Re <b|a>, Im <b|a>].
+template <typename TA, typename TB>
+__global__ void k_compare_partial(const typename Cx<TA>::V2 *a, const typename Cx<TB>::V2 *b, uint64_t dim,
+                                  double *partials) {
+    double mx = 0.0, d2 = 0.0, re = 0.0, im = 0.0;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < dim; i += (uint64_t)gridDim.x * blockDim.x) {
+        const typename Cx<TA>::V2 x = ldg_stream(a + i);
+        const typename Cx<TB>::V2 y = ldg_stream(b + i);
+        const double xr = (double)x.x, xi = (double)x.y, yr = (double)y.x, yi = (double)y.y;
+        const double dr = xr - yr, di = xi - yi, m = dr * dr + di * di;
+        mx = fmax(mx, m);
+        d2 += m;
+        re += yr * xr + yi * xi;
+        im += yr * xi - yi * xr;
+    }
+    __shared__ double wmax[32];
+    for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_down_sync(0xffffffffu, mx, o));
+    if ((threadIdx.x & 31) == 0) wmax[threadIdx.x >> 5] = mx;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        mx = threadIdx.x < ((blockDim.x + 31) >> 5) ? wmax[threadIdx.x] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_down_sync(0xffffffffu, mx, o));
+    }
+    const double s0 = block_sum(d2), s1 = block_sum(re), s2 = block_sum(im);
+    if (threadIdx.x == 0) {
+        partials[blockIdx.x * 4 + 0] = mx;
+        partials[blockIdx.x * 4 + 1] = s0;
+        partials[blockIdx.x * 4 + 2] = s1;
+        partials[blockIdx.x * 4 + 3] = s2;
+    }
+}
+
+// Final reduction of k_compare_partial's slots: component 0 by maximum, 1..3 by fixed-order sums.
+__global__ void k_compare_finalize(const double *partials, int nb, double *result) {
+    __shared__ double wmax[32];
+    double mx = 0.0;
+    for (int i = threadIdx.x; i < nb; i += blockDim.x) mx = fmax(mx, partials[i * 4]);
+    for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_down_sync(0xffffffffu, mx, o));
+    if ((threadIdx.x & 31) == 0) wmax[threadIdx.x >> 5] = mx;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        mx = threadIdx.x < ((blockDim.x + 31) >> 5) ? wmax[threadIdx.x] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_down_sync(0xffffffffu, mx, o));
+        if (threadIdx.x == 0) result[0] = mx;
+    }
+    for (int c = 1; c < 4; ++c) {
+        double acc = 0.0;
+        for (int i = threadIdx.x; i < nb; i += blockDim.x) acc += partials[i * 4 + c];
+        const double r = block_sum(acc);
+        if (threadIdx.x == 0) result[c] = r;
+        __syncthreads();
+    }
+}
+
 // Fixed-order final sum of `nb` partial slots (ncomp components each).
 __global__ void k_finalize(const double *partials, int nb, int ncomp, double *result) {
     for (int c = 0; c < ncomp; ++c) {
@@ -530,6 +585,25 @@ qi_status qi_state_device_ptr(qi_state *s, void **dev_ptr) {
     return publish(ok_status());
 }
 
+qi_status qi_state_wait(qi_state *s, qi_state *other) {
+    if (!other) return publish(err(QI_ERR_NULL_ARGUMENT, -1, -1, "null state"));
+    cudaStream_t theirs;
+    {
+        std::lock_guard<std::recursive_mutex> lk(other->mu);
+        theirs = other->stream;
+    }
+    QI_GUARD(s);
+    if (theirs == s->stream) return publish(ok_status());
+    cudaEvent_t ev;
+    cudaError_t e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+    if (e != cudaSuccess) return publish(cuda_status(e, "cudaEventCreate"));
+    e = cudaEventRecord(ev, theirs);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(s->stream, ev, 0);
+    cudaEventDestroy(ev);   // released once the wait has been satisfied
+    if (e != cudaSuccess) return publish(cuda_status(e, "qi_state_wait"));
+    return publish(ok_status());
+}
+
 qi_status qi_state_synchronize(qi_state *s) {
     QI_GUARD(s);
     cudaError_t e = cudaStreamSynchronize(s->stream);
@@ -770,6 +844,44 @@ qi_status qi_state_inner_product(qi_state *a, qi_state *b, double out[2]) {
     if (a->n != b->n) return publish(err(QI_ERR_INVALID_NUMBER_OF_QUBITS, a->n));   // state.rs:895-897
     if (a->prec != b->prec) return publish(err(QI_ERR_UNSUPPORTED, -1, -1, "inner product needs equal precisions"));
     return publish(state_inner(a, b, out));
+}
+
+qi_status qi_state_compare(qi_state *a, qi_state *b, double out[4]) {
+    QI_GUARD(a);
+    if (!b || !out) return publish(err(QI_ERR_NULL_ARGUMENT));
+    if (a->n != b->n) return publish(err(QI_ERR_INVALID_NUMBER_OF_QUBITS, b->n));
+    if (b->stream != a->stream) {   // order b's pending work before the comparison on a's stream
+        cudaEvent_t ev;
+        cudaError_t e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventRecord(ev, b->stream);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(a->stream, ev, 0);
+        if (e == cudaSuccess) e = cudaEventDestroy(ev);
+        if (e != cudaSuccess) return publish(cuda_status(e, "qi_state_compare"));
+    }
+    const unsigned nb = reduce_grid(a->dim());
+    const bool fa = a->prec == QI_F32, fb = b->prec == QI_F32;
+    if (fa && fb)
+        k_compare_partial<float, float><<<nb, kReduceThreads, 0, a->stream>>>((const float2 *)a->amps,
+                                                                             (const float2 *)b->amps, a->dim(), a->d_partials);
+    else if (fa)
+        k_compare_partial<float, double><<<nb, kReduceThreads, 0, a->stream>>>((const float2 *)a->amps,
+                                                                              (const double2 *)b->amps, a->dim(), a->d_partials);
+    else if (fb)
+        k_compare_partial<double, float><<<nb, kReduceThreads, 0, a->stream>>>((const double2 *)a->amps,
+                                                                              (const float2 *)b->amps, a->dim(), a->d_partials);
+    else
+        k_compare_partial<double, double><<<nb, kReduceThreads, 0, a->stream>>>((const double2 *)a->amps,
+                                                                               (const double2 *)b->amps, a->dim(), a->d_partials);
+    k_compare_finalize<<<1, 256, 0, a->stream>>>(a->d_partials, (int)nb, a->d_result);
+    count_launch(2);
+    Status st = check_launch("k_compare_partial");
+    if (!st.ok()) return publish(st);
+    cudaError_t e = cudaMemcpyAsync(a->h_result, a->d_result, 4 * sizeof(double), cudaMemcpyDeviceToHost, a->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(a->stream);
+    if (e != cudaSuccess) return publish(cuda_status(e, "qi_state_compare"));
+    out[0] = std::sqrt(a->h_result[0]);
+    for (int c = 1; c < 4; ++c) out[c] = a->h_result[c];
+    return publish(ok_status());
 }
 
 qi_status qi_state_norm_sqr(qi_state *s, double *out) {

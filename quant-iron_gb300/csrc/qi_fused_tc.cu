@@ -904,4 +904,101 @@ Status launch_fused_tc(qi_state *s, int k, const int32_t *targets, const void *d
 #undef QI_TC
 }
 
+// ------------------------------------------------------------ rate probe --
+// Dense kind::tf32 rate of this GPU, the tensor roof the fused blocks are reported against:
+// one CTA per SM (the dynamic shared-memory request keeps it alone on its SM), one thread
+// issues `iters` tcgen05.mma M128 x N256 x K8 from the same tensor-memory A operand and
+// shared-memory B block into one accumulator (the pattern of k_fused_tc's product chains),
+// commits and waits.  Operands are zeros; no global memory is touched.
+constexpr int kProbeN = 256, kProbeThreads = 128;
+__global__ void __launch_bounds__(kProbeThreads, 1) k_tf32_rate_probe(int iters, int *err_flag) {
+    __shared__ __align__(1024) float sB[kProbeN * 8];   // N x K = 256 x 8 tf32 (8 KB)
+    __shared__ __align__(8) uint64_t done;
+    __shared__ uint32_t tslot;
+    const int warp = threadIdx.x >> 5;
+    for (int i = threadIdx.x; i < kProbeN * 8; i += blockDim.x) sB[i] = 0.0f;
+    if (threadIdx.x == 0) {
+        mbar_init(&done, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    if (warp == 0) tmem_alloc(&tslot, 512);
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");   // sB visible to the tensor core
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tbase = tslot;
+    {   // A: columns 0..7 of every lane, zeros (warp w writes lanes 32w .. 32w + 31)
+        uint32_t z[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        tmem_st<8>(tbase + ((uint32_t)(warp * 32) << 16), z);
+        tmem_wait_st();
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (threadIdx.x == 0) {
+        // K-major, no swizzle: core matrices (8 rows x 16 B) at 128 B along K, 256 B along N
+        const uint64_t desc = smem_desc(smem_u32(sB), 128, 256);
+        constexpr uint32_t idesc = tf32_idesc(128, kProbeN);
+        const uint32_t d_col = tbase + 256;
+        for (int i = 0; i < iters; ++i) mma_tf32_ts(d_col, tbase, desc, idesc, i > 0 ? 1u : 0u);
+        mma_commit(&done);
+        if (!mbar_wait_bounded(&done, 0)) {
+            atomicExch(err_flag, 2);
+            mbar_wait_bounded(&done, 0);   // once more before the tensor memory is freed
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 0) tmem_dealloc(tbase, 512);
+}
+
 }  // namespace qi
+
+using namespace qi;
+
+extern "C" qi_status qi_tf32_rate_probe(int32_t iters, int32_t reps, double *tflops_out, double *ms_out) {
+    if (!tflops_out) return publish(err(QI_ERR_NULL_ARGUMENT));
+    if (iters < 1 || iters > (1 << 20) || reps < 1 || reps > 1000)
+        return publish(err(QI_ERR_INVALID_INPUT_VALUE, iters, reps, "1 <= iters <= 2^20, 1 <= reps <= 1000"));
+    int dev = 0, sms = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    // 120 KB of dynamic shared memory: one probe CTA per SM, so every CTA gets its 512 columns
+    const int dyn = 120 * 1024;
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_tf32_rate_probe, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn);
+    int *d_flag = nullptr;
+    if (e == cudaSuccess) e = cudaMalloc(&d_flag, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(d_flag, 0, sizeof(int));
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    if (e == cudaSuccess) e = cudaEventCreate(&ev0);
+    if (e == cudaSuccess) e = cudaEventCreate(&ev1);
+    float best = 0.0f;
+    if (e == cudaSuccess) {
+        k_tf32_rate_probe<<<(unsigned)sms, kProbeThreads, dyn>>>(iters, d_flag);   // warm-up
+        count_launch();
+        for (int r = 0; r < reps && e == cudaSuccess; ++r) {
+            e = cudaEventRecord(ev0);
+            k_tf32_rate_probe<<<(unsigned)sms, kProbeThreads, dyn>>>(iters, d_flag);
+            count_launch();
+            if (e == cudaSuccess) e = cudaGetLastError();
+            if (e == cudaSuccess) e = cudaEventRecord(ev1);
+            if (e == cudaSuccess) e = cudaEventSynchronize(ev1);
+            float ms = 0.0f;
+            if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, ev0, ev1);
+            if (e == cudaSuccess && (best == 0.0f || ms < best)) best = ms;
+        }
+    }
+    int flag = 0;
+    if (e == cudaSuccess) e = cudaMemcpy(&flag, d_flag, sizeof(int), cudaMemcpyDeviceToHost);
+    if (ev0) cudaEventDestroy(ev0);
+    if (ev1) cudaEventDestroy(ev1);
+    if (d_flag) cudaFree(d_flag);
+    if (e != cudaSuccess) return publish(cuda_status(e, "qi_tf32_rate_probe"));
+    if (flag) return publish(err(QI_ERR_TIMEOUT, -1, -1, "tf32 rate probe: mbarrier wait timed out"));
+    const double flop = 2.0 * 128.0 * kProbeN * 8.0 * (double)iters * (double)sms;
+    *tflops_out = flop / (best * 1e-3) / 1e12;
+    if (ms_out) *ms_out = best;
+    return publish(ok_status());
+}
+

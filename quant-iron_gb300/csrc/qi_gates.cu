@@ -88,6 +88,16 @@ Status validate_gate(int n, const qi_gate &g) {
         }
         return validate_pauli(n, pt);
     }
+    case QI_GATE_MEASUREMENT: {   // state.rs:543-552
+        if (nt != 0) return err(QI_ERR_INVALID_NUMBER_OF_QUBITS, nt);
+        if (t[0] < QI_BASIS_COMPUTATIONAL || t[0] > QI_BASIS_CUSTOM)
+            return err(QI_ERR_INVALID_INPUT_VALUE, t[0], -1, "measurement basis");
+        if (nc > n) return err(QI_ERR_INVALID_NUMBER_OF_QUBITS, n);
+        for (int k = 0; k < nc; ++k)
+            if (c[k] < 0 || c[k] >= n) return err(QI_ERR_INVALID_QUBIT_INDEX, c[k], n);
+        if ((nc == 0 ? n : nc) > 24) return err(QI_ERR_UNSUPPORTED, nc == 0 ? n : nc, 24, "measuring more than 24 qubits");
+        return ok_status();
+    }
     default:
         return err(QI_ERR_INVALID_INPUT_VALUE, g.kind, -1, "unknown gate kind");
     }
@@ -209,6 +219,18 @@ Status gate_to_matrix(int n, const qi_gate &g, GateMatrix *gm) {
         }
         break;
     }
+    case QI_GATE_MEASUREMENT: {
+        o.nt = 0;
+        o.measure = true;
+        o.controls.clear();
+        o.basis = g.targets[0];
+        o.seed = g.xmask;
+        for (int k = 0; k < g.n_controls; ++k) o.measured.push_back(g.controls[k]);
+        if (o.measured.empty())
+            for (int q = 0; q < n; ++q) o.measured.push_back(q);
+        std::copy(g.params, g.params + 8, o.m);
+        break;
+    }
     default: return err(QI_ERR_INVALID_INPUT_VALUE, g.kind);
     }
     // diagonal?
@@ -235,6 +257,15 @@ Op lower_gate(int n, const GateMatrix &gm) {
         op.zmask = gm.zmask;
         op.alpha_re = gm.alpha_re;
         op.alpha_im = gm.alpha_im;
+        return op;
+    }
+    if (gm.measure) {
+        op.kind = OP_MEASURE;
+        op.mode = gm.basis;
+        op.k = (int32_t)gm.measured.size();
+        for (size_t k = 0; k < gm.measured.size(); ++k) op.perm[k] = (int8_t)gm.measured[k];
+        op.xmask = gm.seed;
+        std::copy(gm.m, gm.m + 8, op.m);
         return op;
     }
     if (gm.nt == 0) { op.kind = OP_NOP; return op; }
@@ -571,6 +602,12 @@ Status launch_op(qi_state *s, const Op &op, const void *d_mats, const void *d_tc
     case OP_PHASE_POLY: {
         if (!d_tc || op.tc_offset < 0) return err(QI_ERR_UNKNOWN, op.kind, -1, "phase polynomial without its block");
         return launch_phase_poly(s, (const float *)d_tc + op.tc_offset);
+    }
+    case OP_MEASURE: {   // Gate::Measurement keeps the collapsed state (gate.rs:104-106)
+        int32_t q[64];
+        for (int k = 0; k < op.k; ++k) q[k] = op.perm[k];
+        uint64_t outcome = 0;
+        return measure_state(s, op.mode, op.m, q, op.k, op.xmask, &outcome, nullptr);
     }
     default:
         return err(QI_ERR_UNKNOWN, op.kind, -1, "unknown op");

@@ -96,6 +96,7 @@ enum OpKind : int32_t {
     OP_PHASE_POLY = 9,    // run of diagonal blocks as one quadratic phase polynomial over all qubits (FP32)
     OP_PAULI_GROUP = 10,  // run of Pauli exponentials with X-masks in {0, X}: parity-indexed table, one pass
     OP_BITPERM = 11,      // run of SWAP / X gates as one qubit permutation: out[j] = in[s(j)] (tiled transpose)
+    OP_MEASURE = 12,      // Gate::Measurement: outcome probabilities, seeded draw, collapse (host-synchronising)
 };
 // OP_PAULI_GROUP limits: diagonal runs use up to kGroupChunks tables of up to
 // 2^kGroupRank factors; pair runs one table of up to 2^kPairRank 2x2 matrices.
@@ -139,6 +140,12 @@ struct GateMatrix {
     bool normalise_after = false;
     uint64_t xmask = 0, zmask = 0;
     double alpha_re = 0, alpha_im = 0;
+    // Gate::Measurement: basis (QI_BASIS_*), measured qubits in outcome-bit order, seed of the
+    // draw (xmask of the gate); m[0..7] = the custom basis matrix
+    bool measure = false;
+    int32_t basis = 0;
+    uint64_t seed = 0;
+    std::vector<int32_t> measured;
 };
 
 // GF(2)-affine index map of a run of X / CNOT / SWAP gates (qi_permute.cu):
@@ -165,6 +172,10 @@ Status state_scratch(qi_state *s, void **out);
 Status state_normalise_device_to_async(qi_state *s, void *out, const void *in);
 
 Status validate_gate(int n, const qi_gate &g);
+// State::measure (state.rs:525-730) on s (caller holds s's mutex): basis change, FP64 outcome
+// probabilities, draw r = uniform01(seed), collapse + renormalise, basis change back.
+Status measure_state(qi_state *s, int basis, const double *custom_u, const int32_t *qubits, int m, uint64_t seed,
+                     uint64_t *outcome_out, double *probs_out);
 // Validate + build the matrix of a (resolved) gate.
 Status gate_to_matrix(int n, const qi_gate &g, GateMatrix *out);
 // Lower a GateMatrix to a single primitive op.

@@ -205,24 +205,12 @@ static uint64_t sample(const std::vector<double> &prob, double r) {   // state.r
     return prob.size() - 1;
 }
 
-}  // namespace qi
-
-using namespace qi;
-
-extern "C" {
-
-qi_status qi_measure(qi_state *s, int32_t basis, const double *custom_u, const int32_t *qubits, int32_t n_qubits,
+Status measure_state(qi_state *s, int basis, const double *custom_u, const int32_t *qubits, int n_qubits,
                      uint64_t seed, uint64_t *outcome_out, double *probs_out) {
-    if (!s || !outcome_out || (n_qubits > 0 && !qubits)) return publish(err(QI_ERR_NULL_ARGUMENT));
-    if (basis < 0 || basis > 3 || (basis == QI_BASIS_CUSTOM && !custom_u))
-        return publish(err(QI_ERR_INVALID_INPUT_VALUE, basis));
-    std::lock_guard<std::recursive_mutex> lk(s->mu);
-    cudaError_t e = cudaSetDevice(s->device);
-    if (e != cudaSuccess) return publish(cuda_status(e, "cudaSetDevice"));
     std::vector<int32_t> all;
     if (n_qubits == 0) { for (int q = 0; q < s->n; ++q) all.push_back(q); qubits = all.data(); n_qubits = s->n; }
     Status st = check_measured(s->n, qubits, n_qubits);
-    if (!st.ok()) return publish(st);
+    if (!st.ok()) return st;
     st = basis_change(s, basis, custom_u, qubits, n_qubits, 0);
     std::vector<double> prob;
     double total = 0.0;
@@ -230,13 +218,13 @@ qi_status qi_measure(qi_state *s, int32_t basis, const double *custom_u, const i
     if (st.ok() && total < 2.220446049250313e-16) st = err(QI_ERR_UNKNOWN, -1, -1, "total probability below f64::EPSILON");
     if (!st.ok()) {
         basis_change(s, basis, custom_u, qubits, n_qubits, 1);   // leave the state as it was
-        return publish(st);
+        return st;
     }
     for (double &x : prob) x = x / total;
     const uint64_t o = sample(prob, uniform01(seed));
     if (prob[o] * total <= 2.220446049250313e-16) {   // the collapsed state would not be normalisable
         basis_change(s, basis, custom_u, qubits, n_qubits, 1);
-        return publish(err(QI_ERR_STATE_NOT_NORMALISED));
+        return err(QI_ERR_STATE_NOT_NORMALISED);
     }
     // required measured bits for outcome o
     uint64_t dmask = 0, want = 0;
@@ -255,10 +243,27 @@ qi_status qi_measure(qi_state *s, int32_t basis, const double *custom_u, const i
         int flag = 0;
         st = state_read_flag(s, &flag);
     }
-    if (!st.ok()) return publish(st);
+    if (!st.ok()) return st;
     *outcome_out = o;
     if (probs_out) std::copy(prob.begin(), prob.end(), probs_out);
-    return publish(ok_status());
+    return ok_status();
+}
+
+}  // namespace qi
+
+using namespace qi;
+
+extern "C" {
+
+qi_status qi_measure(qi_state *s, int32_t basis, const double *custom_u, const int32_t *qubits, int32_t n_qubits,
+                     uint64_t seed, uint64_t *outcome_out, double *probs_out) {
+    if (!s || !outcome_out || (n_qubits > 0 && !qubits)) return publish(err(QI_ERR_NULL_ARGUMENT));
+    if (basis < 0 || basis > 3 || (basis == QI_BASIS_CUSTOM && !custom_u))
+        return publish(err(QI_ERR_INVALID_INPUT_VALUE, basis));
+    std::lock_guard<std::recursive_mutex> lk(s->mu);
+    cudaError_t e = cudaSetDevice(s->device);
+    if (e != cudaSuccess) return publish(cuda_status(e, "cudaSetDevice"));
+    return publish(measure_state(s, basis, custom_u, qubits, n_qubits, seed, outcome_out, probs_out));
 }
 
 qi_status qi_measure_n(qi_state *s, int32_t basis, const double *custom_u, const int32_t *qubits, int32_t n_qubits,

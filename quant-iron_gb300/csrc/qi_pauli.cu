@@ -577,6 +577,24 @@ __global__ void __launch_bounds__(256) k_group_expect(const typename Cx<T>::V2 *
     }
 }
 
+// A group's terms live in dynamic shared memory (24 bytes each).  Above the default 48 KB
+// window (less the kernel's 256 bytes of static block-sum space) the launch needs the
+// opt-in attribute; every caller raises it to the same fixed cap, so concurrent callers
+// never lower it under one another.
+constexpr size_t kGroupExpectSmemCap = 200 * 1024;
+static Status group_expect_smem(bool f32, size_t sm) {
+    if (sm > kGroupExpectSmemCap)
+        return err(QI_ERR_UNSUPPORTED, (int64_t)(sm / sizeof(GroupTerm)), (int64_t)(kGroupExpectSmemCap / sizeof(GroupTerm)),
+                   "too many Pauli terms sharing one X mask for one pass");
+    if (sm + 1024 > 48 * 1024) {
+        if (f32) QI_CUDA(cudaFuncSetAttribute(k_group_expect<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              (int)kGroupExpectSmemCap));
+        else QI_CUDA(cudaFuncSetAttribute(k_group_expect<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)kGroupExpectSmemCap));
+    }
+    return ok_status();
+}
+
 // ---- FP32 states: products and per-thread sums in FP32, folded into FP64
 // every kExpBatch elements, so a pass is bound by memory rather than by the
 // FP64 pipe (FP64 arithmetic runs at a small fraction of the FP32 rate here).
@@ -961,7 +979,7 @@ static Status launch_sumop_apply_f32(qi_state *o, qi_state *in, const std::vecto
                             o->stream));
     QI_CUDA(cudaMemcpyAsync(d_tab, ap.tables.data(), ap.tables.size() * sizeof(float2), cudaMemcpyHostToDevice, o->stream));
     auto kern = k_sumop_apply_f32<IDX>;
-    if (sm > 48 * 1024) QI_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    if (sm + 1024 > 48 * 1024) QI_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     kern<<<pgrid(o->dim()), 256, sm, o->stream>>>((float2 *)o->amps, (const float2 *)in->amps, o->dim(), d_hdr,
                                                  (int)ap.hdrs.size(), d_term, (int)ap.terms.size(), d_tab, ap.ntables);
     count_launch();
@@ -1024,7 +1042,9 @@ Status sumop_expectation(qi_state *s, const qi_pauli_term *terms, int64_t nt, do
     const bool f32 = s->prec == QI_F32;
     std::vector<void *> scratch;   // per-call device tables, freed (stream-ordered) at the end
     for (const GroupHdr &h : hdrs) {
-        if (f32 && (size_t)h.count * sizeof(GroupTerm) <= 48 * 1024) {
+        // FP32 kernels keep a group's terms in the default 48 KB shared-memory window (less their
+        // static block-sum space); larger groups take k_group_expect below
+        if (f32 && (size_t)h.count * sizeof(GroupTerm) + 1024 <= 48 * 1024) {
             const GroupTerm *gt = gts.data() + h.first;
             unsigned nb = 1;
             if (h.xmask == 0) {
@@ -1114,6 +1134,8 @@ Status sumop_expectation(qi_state *s, const qi_pauli_term *terms, int64_t nt, do
         uint64_t nb64 = (work + kReduceThreads - 1) / kReduceThreads;
         const unsigned nb = (unsigned)std::min<uint64_t>(std::max<uint64_t>(nb64, 1), kReduceBlocks);
         const size_t sm = (size_t)h.count * sizeof(GroupTerm);
+        st = group_expect_smem(f32, sm);
+        if (!st.ok()) return st;
         if (f32)
             k_group_expect<float><<<nb, kReduceThreads, sm, s->stream>>>((const float2 *)s->amps, s->dim(), h, d_terms,
                                                                          s->d_partials);
@@ -1153,11 +1175,11 @@ Status sumop_apply(qi_state *o, qi_state *in, const qi_pauli_term *terms, int64_
     if (sm > 200 * 1024) return err(QI_ERR_UNSUPPORTED, (int64_t)nt, -1, "too many Pauli terms for one pass");
     unsigned g = pgrid(o->dim());
     if (o->prec == QI_F32) {
-        if (sm > 48 * 1024) QI_CUDA(cudaFuncSetAttribute(k_sumop_apply<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        if (sm + 1024 > 48 * 1024) QI_CUDA(cudaFuncSetAttribute(k_sumop_apply<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
         k_sumop_apply<float><<<g, 256, sm, o->stream>>>((float2 *)o->amps, (const float2 *)in->amps, o->dim(), d_hdr,
                                                        (int)hdrs.size(), d_terms, (int)gts.size());
     } else {
-        if (sm > 48 * 1024) QI_CUDA(cudaFuncSetAttribute(k_sumop_apply<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        if (sm + 1024 > 48 * 1024) QI_CUDA(cudaFuncSetAttribute(k_sumop_apply<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
         k_sumop_apply<double><<<g, 256, sm, o->stream>>>((double2 *)o->amps, (const double2 *)in->amps, o->dim(), d_hdr,
                                                         (int)hdrs.size(), d_terms, (int)gts.size());
     }
@@ -1310,7 +1332,7 @@ qi_status qi_sumop_expectation(qi_state *s, const qi_pauli_term *terms, int64_t 
 namespace qi {
 
 constexpr int kNoAllocMaxTerms = 4096;
-constexpr int kNoAllocMaxGroupTerms = 2048;   // 48 KB of shared memory per group kernel
+constexpr int kNoAllocMaxGroupTerms = 2048;   // 48 KB of dynamic shared memory per group kernel
 constexpr size_t kNoAllocPartialsOff = 0;
 constexpr size_t kNoAllocResultOff = (size_t)kReduceBlocks * 4 * sizeof(double);        // 38912, 256-aligned
 constexpr size_t kNoAllocTermsOff = kNoAllocResultOff + 256;
@@ -1321,19 +1343,46 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratch
 static std::mutex g_noalloc_mu;
 static void *g_noalloc_ptr[64] = {nullptr};   // device address of g_noalloc_scratch, per device ordinal
 
-// Device address of the scratch array on the current device (set-up on the
-// first call per device: cudaGetSymbolAddress with that device current).
-static Status noalloc_scratch(void **out) {
-    int dev = 0;
-    QI_CUDA(cudaGetDevice(&dev));
+// Device address of the scratch array on the current device.  Set-up on the first call per
+// device, with that device current: cudaGetSymbolAddress, and the shared-memory opt-in of the
+// group kernels (a group of kNoAllocMaxGroupTerms terms needs 48 KB of dynamic shared memory
+// plus the kernel's static block-sum space, just above the default window).  The address is
+// cached for the life of the process; a cudaDeviceReset between calls is not supported.
+static Status noalloc_scratch(int dev, void **out) {
     if (dev < 0 || dev >= 64) return err(QI_ERR_UNSUPPORTED, dev, -1, "device ordinal above 63");
     std::lock_guard<std::mutex> lk(g_noalloc_mu);
     if (!g_noalloc_ptr[dev]) {
         void *p = nullptr;
         QI_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+        Status st = group_expect_smem(true, (size_t)kNoAllocMaxGroupTerms * sizeof(GroupTerm));
+        if (st.ok()) st = group_expect_smem(false, (size_t)kNoAllocMaxGroupTerms * sizeof(GroupTerm));
+        if (!st.ok()) return st;
         g_noalloc_ptr[dev] = p;
     }
     *out = g_noalloc_ptr[dev];
+    return ok_status();
+}
+
+// The caller's buffer and stream must belong to the current device (the scratch address
+// is the current device's).
+static Status noalloc_check_device(int dev, const void *amps, cudaStream_t stream) {
+    cudaPointerAttributes pa;
+    cudaError_t e = cudaPointerGetAttributes(&pa, amps);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return err(QI_ERR_INVALID_INPUT_VALUE, -1, dev, "qi_sumop_expectation_noalloc: amps is not a device pointer");
+    }
+    if ((pa.type != cudaMemoryTypeDevice && pa.type != cudaMemoryTypeManaged) || pa.device != dev)
+        return err(QI_ERR_INVALID_INPUT_VALUE, pa.device, dev,
+                   "qi_sumop_expectation_noalloc: amps must be device memory of the current device");
+    if (stream) {
+        int sdev = -1;
+        e = cudaStreamGetDevice(stream, &sdev);
+        if (e != cudaSuccess) return cuda_status(e, "qi_sumop_expectation_noalloc: cudaStreamGetDevice");
+        if (sdev != dev)
+            return err(QI_ERR_INVALID_INPUT_VALUE, sdev, dev,
+                       "qi_sumop_expectation_noalloc: cuda_stream belongs to another device");
+    }
     return ok_status();
 }
 
@@ -1384,10 +1433,15 @@ extern "C" qi_status qi_sumop_expectation_noalloc(const void *amps, int32_t num_
         t.im = terms[k].coeff_re * pi + terms[k].coeff_im * pr;
         packed[gfirst[gi] + gcount[gi]++] = t;
     }
-    void *scratch = nullptr;
-    Status st = noalloc_scratch(&scratch);
-    if (!st.ok()) return publish(st);
     cudaStream_t stream = (cudaStream_t)cuda_stream;
+    int dev = 0;
+    cudaError_t de = cudaGetDevice(&dev);
+    if (de != cudaSuccess) return publish(cuda_status(de, "cudaGetDevice"));
+    Status st = noalloc_check_device(dev, amps, stream);
+    if (!st.ok()) return publish(st);
+    void *scratch = nullptr;
+    st = noalloc_scratch(dev, &scratch);
+    if (!st.ok()) return publish(st);
     double *partials = (double *)((char *)scratch + kNoAllocPartialsOff);
     double *result = (double *)((char *)scratch + kNoAllocResultOff);
     GroupTerm *d_terms = (GroupTerm *)((char *)scratch + kNoAllocTermsOff);

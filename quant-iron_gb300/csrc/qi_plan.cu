@@ -46,6 +46,12 @@ Elem make_elem_from_gate(const GateMatrix &gm, int src) {
     Elem e;
     e.src = src;
     e.gm = gm;
+    if (gm.measure) {   // a barrier: nothing is fused or reordered across a measurement
+        e.mask = ~0ull;
+        e.diagonal = false;
+        e.fusable = false;
+        return e;
+    }
     if (gm.pauli) {
         const uint64_t sup = gm.xmask | gm.zmask;
         e.mask = gm.normalise_after ? ~0ull : sup;
@@ -579,6 +585,10 @@ struct PlanRunner {
             if (st.ok()) s->amps = dst;
             return st;
         }
+        if (o.kind == OP_MEASURE && s->amps != home) {   // measure the amplitudes in the state's own buffer
+            Status st = finish(ok_status());
+            if (!st.ok()) return st;
+        }
         if (o.kind == OP_NORMALISE && s->amps != home) {
             Status st = state_normalise_device_to_async(s, home, s->amps);
             if (st.ok()) s->amps = home;
@@ -841,6 +851,11 @@ qi_status qi_plan_op_get(const qi_plan *p, int64_t i, qi_plan_op_info *info, dou
         break;
     }
     case OP_PAULI_EXP: m = {op.cre, op.cim, op.sre, op.sim}; break;
+    case OP_MEASURE:   // k measured qubits (the first six in targets), basis in zmask, seed in xmask
+        for (int j = 0; j < 6; ++j) info->targets[j] = j < op.k ? op.perm[j] : 0;
+        info->zmask = (uint64_t)op.mode;
+        if (op.mode == QI_BASIS_CUSTOM) m.assign(op.m, op.m + 8);
+        break;
     case OP_PAULI_GROUP: {
         size_t cnt = 0;
         for (int c = 0; c < op.nchunk; ++c) cnt += (size_t)(op.xmask ? 4 : 1) << op.rank[c];

@@ -576,6 +576,17 @@ class Gate:
         return Gate(op.gate_row(targets, controls))
 
     @staticmethod
+    def new_measurement(qubit_indices, basis=None, seed=0):
+        """Gate::new_measurement (gate.rs:63-65): State::measure in `basis` on the qubits (all
+        of them when empty), keeping the collapsed state; `seed` seeds the outcome draw (the
+        reference's draw is unseeded)."""
+        name, u = _basis_args(basis)
+        code = {"Computational": 0, "X": 1, "Y": 2, "Custom": 3}[name]
+        return Gate(GateList().measure(list(qubit_indices), code, u, seed).array()[0])
+
+    measurement = new_measurement
+
+    @staticmethod
     def pauli_string(ps):
         x, z = ps.masks()
         gl = GateList().add("PAULI_STRING", [], [], [ps.coefficient.real, ps.coefficient.imag], xmask=x, zmask=z)

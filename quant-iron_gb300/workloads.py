@@ -14,7 +14,7 @@ import math
 
 import numpy as np
 
-from ._abi import GATE_DTYPE, GATE_KINDS, TERM_DTYPE
+from ._types import GATE_DTYPE, GATE_KINDS, TERM_DTYPE
 
 ONE_QUBIT_SET = ["H", "X", "Y", "Z", "S", "T", "RX", "RY", "RZ", "P"]
 PARAMETRIC = {"RX", "RY", "RZ", "P"}
@@ -38,6 +38,24 @@ class GateList:
         g["param_ids"][:len(param_ids)] = param_ids
         g["xmask"] = xmask
         g["zmask"] = zmask
+        self._rows.append(g)
+        return self
+
+    def measure(self, qubits, basis=0, custom=None, seed=0):
+        """Gate::Measurement(basis, qubits): basis 0 computational, 1 X, 2 Y, 3 custom (2x2
+        complex matrix `custom`); `seed` seeds the outcome draw."""
+        g = np.zeros((), dtype=GATE_DTYPE)
+        g["kind"] = GATE_KINDS["MEASUREMENT"]
+        g["n_targets"] = 0
+        g["targets"][0] = int(basis)
+        g["n_controls"] = len(qubits)
+        g["controls"][:len(qubits)] = qubits
+        g["param_ids"][:] = -1
+        if custom is not None:
+            u = np.asarray(custom, dtype=np.complex128).reshape(4)
+            g["params"][0::2] = u.real
+            g["params"][1::2] = u.imag
+        g["xmask"] = np.uint64(seed)
         self._rows.append(g)
         return self
 

@@ -1,8 +1,8 @@
 """Adjoint gradient vs FP64 central finite differences and parameter shift (GPU).
 
-Norm-wise relative error ||g - g_ref|| / ||g_ref||: <= 1e-6 with an FP64
-state (the benchmark spec's bound), <= 1e-4 with an FP32 state (FP32 rounding of
-~1e3 gate applications); finite differences use eps = 1e-4 on the FP64 oracle."""
+Norm-wise relative error ||g - g_ref|| / ||g_ref|| <= 1e-6 (the benchmark spec's bound)
+with an FP64 and with an FP32 state; finite differences use eps = 1e-4 in FP64 (the
+oracle, or the engine's plain FP64 per-gate path at 20 and more qubits)."""
 import numpy as np
 import pytest
 
@@ -25,7 +25,7 @@ def fd_grad(orc, n, gates, theta, terms, init, ids, eps=1e-4):
     return g
 
 
-@pytest.mark.parametrize("prec,tol", [(0, 1e-6), (1, 1e-4)], ids=["f64", "f32"])
+@pytest.mark.parametrize("prec,tol", [(0, 1e-6), (1, 1e-6)], ids=["f64", "f32"])
 def test_hea_gradient_vs_finite_differences(qi, orc, prec, tol):
     n = 8
     gates, theta = workloads.hea_ansatz(n, layers=3, seed=1)
@@ -41,8 +41,8 @@ def test_hea_gradient_vs_finite_differences(qi, orc, prec, tol):
     g_ref = fd_grad(orc, n, gates, theta, terms, init, ids)
     rel = np.linalg.norm(g - g_ref) / np.linalg.norm(g_ref)
     assert rel < tol, rel
-    # the reverse sweep restores the initial state
-    assert np.max(np.abs(back - init)) < (1e-12 if prec == 0 else 1e-5)
+    # the caller's state is untouched (the sweep runs on a copy)
+    assert np.array_equal(back, init)
 
 
 def test_parameter_shift_rotations(qi, orc):
@@ -109,8 +109,45 @@ def test_adjoint_26q_fp32_vs_fp64_gpu(qi):
             e, g = qi.adjoint_gradient(st, gates, theta, terms)
             grads[prec] = (e, g)
     rel = np.linalg.norm(grads[1][1] - grads[0][1]) / np.linalg.norm(grads[0][1])
-    assert rel < 1e-4, rel
-    assert abs(grads[1][0] - grads[0][0]) < 1e-4
+    assert rel < 1e-6, rel
+    assert abs(grads[1][0] - grads[0][0]) < 1e-6
+
+
+def gpu_fd_grad(qi, n, gates, theta, terms, eps=1e-4):
+    """FP64 central differences of E on every parameter with the plain FP64 per-gate path."""
+    g = np.zeros(theta.size)
+    with qi.DeviceState(n, 0) as st:
+        for j in range(theta.size):
+            e = []
+            for sgn in (1.0, -1.0):
+                th = theta.copy()
+                th[j] += sgn * eps
+                st.set_zero()
+                qi.Plan(n, 0, gates, theta=th, fusion=qi.FUSION_NONE).execute(st)
+                e.append(qi.sumop_expectation(st, terms).real)
+            g[j] = (e[0] - e[1]) / (2 * eps)
+    return g
+
+
+def test_hea20_fp32_adjoint_within_1e6_of_finite_differences(qi):
+    """20 qubits, 12 layers (480 parameters), periodic XXZ: the FP32-state adjoint gradient
+    within 1e-6 (norm-wise) of FP64 central differences on all parameters, and the
+    FP64-state adjoint within 1e-8; calling twice on the same state gives the same result."""
+    n = 20
+    gates, theta = workloads.hea_ansatz(n, layers=12, seed=1)
+    terms = workloads.xxz_periodic(n, seed=1)
+    g_fd = gpu_fd_grad(qi, n, gates, theta, terms)
+    out = {}
+    for prec in (0, 1):
+        with qi.DeviceState(n, prec) as st:
+            st.set_zero()
+            out[prec] = qi.adjoint_gradient(st, gates, theta, terms)[1]
+            again = qi.adjoint_gradient(st, gates, theta, terms)[1]
+            assert np.array_equal(again, out[prec])
+    rel64 = np.linalg.norm(out[0] - g_fd) / np.linalg.norm(g_fd)
+    rel32 = np.linalg.norm(out[1] - g_fd) / np.linalg.norm(g_fd)
+    assert rel64 < 1e-8, rel64
+    assert rel32 < 1e-6, rel32
 
 
 def grouped_sweep_circuit(n, n_runs, seed):
@@ -162,8 +199,9 @@ def grouped_sweep_circuit(n, n_runs, seed):
 def test_grouped_reverse_sweep_vs_per_gate_and_fd(qi, orc, n):
     """Single-qubit groups and fused fixed runs in the reverse sweep: FP64 gradients equal
     the per-gate sweep (fusion off) to 1e-10, match FP64 finite differences of the oracle
-    to 1e-6 on a seeded subset, FP32 stays within 1e-4 of FP64, and both sweeps restore
-    the initial state."""
+    to 1e-6 on a seeded subset, FP32 stays within 1e-5 of FP64 (these circuits carry controlled
+    and fixed gates whose FP32 rounding the sweep does not divide out), and the caller's
+    state is left as it was."""
     gates, theta = grouped_sweep_circuit(n, 6, seed=n)
     terms = workloads.xxz_periodic(n, seed=2)
     init = workloads.plus_state(n)
@@ -173,12 +211,12 @@ def test_grouped_reverse_sweep_vs_per_gate_and_fd(qi, orc, n):
             st.upload(init)
             e, g = qi.adjoint_gradient(st, gates, theta, terms, fusion=fusion)
             back = st.download()
-        assert np.max(np.abs(back - init)) < (1e-12 if prec == 0 else 1e-5)
+        assert np.array_equal(back, init)
         res[(prec, fusion)] = (e, g)
     g_none, g64 = res[(0, qi.FUSION_NONE)][1], res[(0, qi.FUSION_GREEDY)][1]
     assert np.linalg.norm(g64 - g_none) / np.linalg.norm(g_none) < 1e-10
     g32 = res[(1, qi.FUSION_GREEDY)][1]
-    assert np.linalg.norm(g32 - g64) / np.linalg.norm(g64) < 1e-4
+    assert np.linalg.norm(g32 - g64) / np.linalg.norm(g64) < 1e-5
     rng = np.random.default_rng(5)
     ids = sorted(int(x) for x in rng.choice(theta.size, min(12, theta.size), replace=False))
     g_ref = fd_grad(orc, n, gates, theta, terms, init, ids)
@@ -190,8 +228,8 @@ def test_grouped_reverse_sweep_vs_per_gate_and_fd(qi, orc, n):
 def test_permutation_runs_in_reverse_sweep(qi, orc, layers, prec):
     """Runs of X / CNOT / SWAP / singly-controlled X between rotation layers are un-applied
     as one index permutation per state (psi and lambda move between three buffers; an odd
-    number of runs leaves psi in another buffer, which the call copies back): gradients
-    equal the per-gate sweep and the state returns to the initial one."""
+    number of runs leaves psi in another buffer): gradients equal the per-gate sweep and the
+    caller's state is left as it was."""
     n = 11
     rng = np.random.default_rng(layers)
     gl = workloads.GateList()
@@ -216,10 +254,10 @@ def test_permutation_runs_in_reverse_sweep(qi, orc, layers, prec):
             st.upload(init)
             e, g = qi.adjoint_gradient(st, gates=gl.array(), theta=theta, terms=terms, fusion=fusion)
             back = st.download()
-        assert np.max(np.abs(back - init)) < (1e-12 if prec == 0 else 1e-5)
+        assert np.array_equal(back, init)
         res[fusion] = (e, g)
     (e0, g0), (e1, g1) = res[qi.FUSION_NONE], res[qi.FUSION_GREEDY]
-    assert np.linalg.norm(g1 - g0) / np.linalg.norm(g0) < (1e-10 if prec == 0 else 1e-4)
+    assert np.linalg.norm(g1 - g0) / np.linalg.norm(g0) < (1e-10 if prec == 0 else 1e-5)
     if prec == 0:
         e_ref = energy_oracle(orc, n, gl.array(), theta, terms, init)
         assert abs(e1 - e_ref) < 1e-12
@@ -254,7 +292,7 @@ def test_pauli_exponential_inside_a_cnot_swap_run(qi, orc, prec):
             st.upload(init)
             res[fusion] = qi.adjoint_gradient(st, gates, theta, terms, fusion=fusion)[1]
     g0, g1 = res[qi.FUSION_NONE], res[qi.FUSION_GREEDY]
-    assert np.linalg.norm(g1 - g0) / np.linalg.norm(g0) < (1e-10 if prec == 0 else 1e-4)
+    assert np.linalg.norm(g1 - g0) / np.linalg.norm(g0) < (1e-10 if prec == 0 else 1e-5)
     if prec == 0:
         ids = list(range(npar))
         g_ref = fd_grad(orc, n, gates, theta, terms, init, ids)

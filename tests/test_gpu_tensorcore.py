@@ -153,3 +153,14 @@ def test_tensor_core_norm_drift_and_renormalisation(qi):
             norms[renorm] = st.norm_sqr()
     assert abs(norms[0] - 1.0) < 1e-6 and abs(norms[5] - 1.0) < 1e-6
     assert abs(norms[-1] - 1.0) < 1e-3   # drift without renormalisation stays small
+
+
+def test_tf32_rate_probe(qi):
+    """The tensor roof probe runs, reports a rate in the range of a GB300's dense TF32
+    (nominal 1.1 PFLOP/s) and leaves the device usable."""
+    tf, ms = qi.tf32_rate_probe(iters=4096, reps=2)
+    assert 100.0 < tf < 3000.0, tf
+    assert ms > 0.0
+    with qi.DeviceState(14, qi.F32) as st:
+        st.set_plus()
+        assert abs(st.norm_sqr() - 1.0) < 1e-6

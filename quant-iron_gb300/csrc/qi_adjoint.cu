@@ -520,7 +520,8 @@ static void fill_adj_positions(AdjParams &p, const GateMatrix &gm, uint64_t cmas
 // [[a, -conj(b)], [b, conj(a)]] are rounded.  Un-applying then scales psi and lambda by
 // exactly r, a deterministic drift of up to ~1e-7 per stage that the host divides out of
 // the gradient instead of letting it accumulate over the sweep.
-static double fp32_stage_matrix(double *u) {
+static double fp32_stage_matrix(double *u, std::complex<double> *phase = nullptr) {
+    if (phase) *phase = 1.0;
     double f[8];
     for (int i = 0; i < 8; ++i) f[i] = (double)(float)u[i];
     auto dot = [&](int a, int b, double &re, double &im) {   // conj(col a) . col b
@@ -541,6 +542,7 @@ static double fp32_stage_matrix(double *u) {
     const std::complex<double> u00(u[0], u[1]), u01(u[2], u[3]), u10(u[4], u[5]), u11(u[6], u[7]);
     const std::complex<double> ph = std::exp(std::complex<double>(0.0, -0.5 * std::arg(u00 * u11 - u01 * u10)));
     const std::complex<double> a = u00 * ph, b = u10 * ph;
+    if (phase) *phase = ph;
     const double ar = (float)a.real(), ai = (float)a.imag(), br = (float)b.real(), bi = (float)b.imag();
     u[0] = ar; u[1] = ai; u[2] = -br; u[3] = bi;
     u[4] = br; u[5] = bi; u[6] = ar; u[7] = -ai;
@@ -769,6 +771,9 @@ extern "C" qi_status qi_adjoint_gradient(qi_state *s, const qi_gate *gates, int6
     // scales (fp32_stage_matrix) multiply in; after a tensor-core plan segment (which rounds
     // toward zero) both are measured.  A derivative term is divided by sqrt(cpsi * clam).
     double cpsi = 1.0, clam = 1.0, npsi0 = 1.0, nlam0 = 1.0;
+    // (the exact-scale matrices may carry a global phase into psi: only when psi_0 is not the
+    // state the sweep hands back)
+    const bool scale_fix = f32 && work != nullptr;
     if (st.ok() && f32) st = state_reduce_norm_sqr(s, &npsi0);
     if (st.ok() && f32 && n_terms > 0) st = state_reduce_norm_sqr(lam, &nlam0);
     if (!(npsi0 > 0.0)) npsi0 = 1.0;
@@ -833,7 +838,7 @@ extern "C" qi_status qi_adjoint_gradient(qi_state *s, const qi_gate *gates, int6
                         dd[2 * (2 * r + c)] = re;
                         dd[2 * (2 * r + c) + 1] = im;
                     }
-                if (f32) r2[b][t] = fp32_stage_matrix(ui);
+                if (scale_fix) r2[b][t] = fp32_stage_matrix(ui);
                 bool diag = true, real = true;
                 for (int e = 0; e < 8; ++e) {
                     const bool off = e == 2 || e == 3 || e == 4 || e == 5;
@@ -966,8 +971,19 @@ extern "C" qi_status qi_adjoint_gradient(qi_state *s, const qi_gate *gates, int6
         for (int q = 0; q < nd && st.ok(); ++q) st = derivative_matrix(n, g, ids[q], p.d[q]);
         if (!st.ok()) break;
         // an uncontrolled single-qubit stage scales both states by exactly r (FP32); the term
-        // uses psi after the un-apply and lambda before it
-        const double r2g = (f32 && gm.nt == 1 && cm == 0) ? fp32_stage_matrix(p.uinv) : 1.0;
+        // uses psi after the un-apply and lambda before it, so a global phase ph taken into
+        // U^dagger is taken out of dU (conj(ph) dU U^dagger ph = dU U^dagger)
+        double r2g = 1.0;
+        if (scale_fix && gm.nt == 1 && cm == 0) {
+            std::complex<double> ph;
+            r2g = fp32_stage_matrix(p.uinv, &ph);
+            for (int q = 0; q < nd; ++q)
+                for (int e2 = 0; e2 < 4; ++e2) {
+                    const std::complex<double> v = std::complex<double>(p.d[q][2 * e2], p.d[q][2 * e2 + 1]) * std::conj(ph);
+                    p.d[q][2 * e2] = v.real();
+                    p.d[q][2 * e2 + 1] = v.imag();
+                }
+        }
         const double facg = 1.0 / std::sqrt(cpsi * r2g * clam);
         cpsi *= r2g;
         clam *= r2g;

@@ -397,6 +397,28 @@ __global__ void __launch_bounds__(256) k_mat1(typename Cx<T>::V2 *a, GateParams 
     }
 }
 
+// One target on qubit 0 (FP32): a pair (i0, i0 + 1) is one 16-byte load and store, so a
+// warp moves 512 contiguous bytes per instruction (the generic path's two 8-byte accesses
+// per pair sit 8 bytes apart).  Two pairs per thread are in flight.
+template <int MODE, int PH>
+__global__ void __launch_bounds__(256) k_mat1_q0(float2 *a, GateParams p) {
+    const Mat1Coef<float> c(p.m);
+    float4 *a4 = reinterpret_cast<float4 *>(a);
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t w = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; w < p.nwork; w += 2 * stride) {
+        const bool two = w + stride < p.nwork;
+        const uint64_t j0 = (insert_zeros(w, p.pos, p.np) | p.cmask) >> 1;
+        const uint64_t j1 = two ? (insert_zeros(w + stride, p.pos, p.np) | p.cmask) >> 1 : j0;
+        float4 u = a4[j0], v = two ? a4[j1] : u;
+        float2 x0 = make_float2(u.x, u.y), y0 = make_float2(u.z, u.w);
+        float2 x1 = make_float2(v.x, v.y), y1 = make_float2(v.z, v.w);
+        mat1_update<float, MODE, PH>(x0, y0, c);
+        mat1_update<float, MODE, PH>(x1, y1, c);
+        a4[j0] = make_float4(x0.x, x0.y, y0.x, y0.y);
+        if (two) a4[j1] = make_float4(x1.x, x1.y, y1.x, y1.y);
+    }
+}
+
 template <typename T, bool VEC>
 __global__ void __launch_bounds__(256) k_swap(typename Cx<T>::V2 *a, GateParams p) {
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
@@ -499,6 +521,27 @@ static int phase_kind(const Op &op) {
     return PH_GENERAL;
 }
 
+static void launch_mat1_q0(float2 *a, const GateParams &p, int mode, int ph, unsigned g, cudaStream_t st) {
+#define QI_M1(MODE, PH) k_mat1_q0<MODE, PH><<<g, 256, 0, st>>>(a, p)
+    switch (mode) {
+    case M1_GENERAL: QI_M1(M1_GENERAL, PH_GENERAL); break;
+    case M1_REAL: QI_M1(M1_REAL, PH_GENERAL); break;
+    case M1_DIAG: QI_M1(M1_DIAG, PH_GENERAL); break;
+    case M1_ANTIDIAG:
+        if (ph == PH_NEG) QI_M1(M1_ANTIDIAG, PH_NEG);
+        else if (ph == PH_I) QI_M1(M1_ANTIDIAG, PH_I);
+        else QI_M1(M1_ANTIDIAG, PH_GENERAL);
+        break;
+    default:
+        if (ph == PH_NEG) QI_M1(M1_PHASE1, PH_NEG);
+        else if (ph == PH_I) QI_M1(M1_PHASE1, PH_I);
+        else if (ph == PH_NEG_I) QI_M1(M1_PHASE1, PH_NEG_I);
+        else QI_M1(M1_PHASE1, PH_GENERAL);
+        break;
+    }
+#undef QI_M1
+}
+
 template <typename T, bool VEC>
 static void launch_mat1_t(typename Cx<T>::V2 *a, const GateParams &p, int mode, int ph, unsigned g, cudaStream_t st) {
 #define QI_M1(MODE, PH) k_mat1<T, MODE, PH, VEC><<<g, 256, 0, st>>>(a, p)
@@ -539,7 +582,9 @@ Status launch_op(qi_state *s, const Op &op, const void *d_mats, const void *d_tc
         p.nwork = 1ull << (free_bits - (vec ? 1 : 0));
         const unsigned g = gate_grid(p.nwork);
         const int ph = phase_kind(op);
-        if (f32) {
+        if (f32 && op.targets[0] == 0) {   // pairs are adjacent: one 16-byte access each
+            launch_mat1_q0((float2 *)s->amps, p, op.mode, ph, gate_grid((p.nwork + 1) / 2), s->stream);
+        } else if (f32) {
             if (vec) launch_mat1_t<float, true>((float2 *)s->amps, p, op.mode, ph, g, s->stream);
             else launch_mat1_t<float, false>((float2 *)s->amps, p, op.mode, ph, g, s->stream);
         } else {

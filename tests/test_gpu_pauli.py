@@ -239,3 +239,30 @@ def test_grouped_exponentials_32_qubits_round_trip(qi):
         assert abs(st.inner_product(ref)) < 0.999   # the run moved the state
         back.execute(st)
         assert abs(st.inner_product(ref) - 1.0) < 1e-4
+
+
+@pytest.mark.parametrize("model", ["heisenberg", "tfim"])
+def test_fp32_trotter_energy_error_20q_20_steps(qi, orc, model):
+    """The FP32 fused Trotter method on a 4x5 lattice (20 qubits), 20 first-order steps of
+    dt = 0.05 from a seeded basis state, against the oracle's FP64 steps
+    (time_evolution.rs:45-66): <H> after 10 and 20 steps within 2e-6 relative to the
+    Hamiltonian's coefficient scale (sum |c_k|), state infidelity within 1e-8.  The error
+    comes from the tensor-core blocks' FP32 accumulation (round toward zero) and grows
+    about linearly with the number of steps."""
+    rows, cols, n = 4, 5, 20
+    terms = workloads.lattice_xyz(rows, cols, seed=3) if model == "heisenberg" else \
+        workloads.lattice_tfim(rows, cols, seed=3)
+    basis = int(np.random.default_rng(3).integers(0, 1 << n))
+    init = workloads.basis_state(n, basis)
+    scale = float(np.sum(np.abs(terms["re"])))
+    want10 = orc.trotter(init, n, terms, 0.05, 10, 1)
+    want20 = orc.trotter(want10, n, terms, 0.05, 10, 1)
+    e_want = [orc.sumop_expectation(w, n, terms).real for w in (want10, want20)]
+    with qi.DeviceState(n, qi.F32) as st:
+        st.set_basis(basis)
+        e_got = [complex(x).real for x in qi.trotter_evolve(st, terms, 0.05, 20, observable=terms, observe_every=10)]
+        got = st.download()
+    for a, b in zip(e_got, e_want):
+        assert abs(a - b) < 2e-6 * scale, (a, b, scale)
+    infid = 1.0 - abs(np.vdot(want20, got)) ** 2 / (np.vdot(got, got).real * np.vdot(want20, want20).real)
+    assert infid < 1e-8, infid

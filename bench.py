@@ -53,8 +53,12 @@ def parse():
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
     ap.add_argument("--qubits", type=int, default=N_QUBITS)
     ap.add_argument("--skip-baselines", action="store_true", help="skip FP64/FP32 per-gate and CPU legs")
+    ap.add_argument("--costmodel-eval", action="store_true",
+                    help="run the learned-fusion evaluation (4000 timings at 28 qubits, circuits of 28-34 qubits) "
+                         "instead of the benchmark")
     ap.add_argument("--adjoint-fd", default="subset", choices=["subset", "all"],
-                    help="finite differences / parameter shift on a seeded subset (64 / 32 parameters) or on all 624")
+                    help="FP64 central differences on a seeded 64-parameter subset, or (all) on all 624 "
+                         "parameters, running the adjoint configuration alone")
     ap.add_argument("--profile-case", default=None, choices=["fused26", "trotter26", "adjoint26"],
                     help="run a small fixed case for ncu captures instead of the benchmark")
     return ap.parse_args()
@@ -278,8 +282,8 @@ def adjoint_leg(qi, workloads, stream, torch, np, n=26, layers=12, fd="subset"):
     """Adjoint gradient of the 26-qubit hardware-efficient ansatz (12 layers of RY.RZ + CNOT
     ladder, 624 parameters, seed 1) on the periodic XXZ energy (104 terms): gradients/s with an
     FP32 state; the FP32 and FP64 adjoints on all 624 parameters; FP64 central differences
-    (eps 1e-4) and parameter shift (+-pi/2) from the plain FP64 per-gate path, on a seeded
-    subset (fd="subset": 64 and 32 parameters) or on every parameter (fd="all")."""
+    (eps 1e-4) on a seeded 64-parameter subset (fd="all": on every parameter) and parameter shift
+    (+-pi/2) on a seeded 32-parameter subset, both from the plain FP64 per-gate path."""
     gates, theta = workloads.hea_ansatz(n, layers, seed=1)
     terms = workloads.xxz_periodic(n, seed=1)
     s32 = qi.DeviceState(n, qi.F32)
@@ -303,12 +307,10 @@ def adjoint_leg(qi, workloads, stream, torch, np, n=26, layers=12, fd="subset"):
     t64 = time.perf_counter() - t0
     s64.close()
     rng = np.random.default_rng(1)
+    fd_ids = np.sort(rng.choice(theta.size, 64, replace=False))
+    ps_ids = np.sort(rng.choice(theta.size, 32, replace=False))
     if fd == "all":
         fd_ids = np.arange(theta.size)
-        ps_ids = np.arange(theta.size)
-    else:
-        fd_ids = np.sort(rng.choice(theta.size, 64, replace=False))
-        ps_ids = np.sort(rng.choice(theta.size, 32, replace=False))
     t0 = time.perf_counter()
     ev = fd_energies(qi, n, gates, theta, terms, fd_ids, (1e-4, -1e-4), stream)
     ev.update(fd_energies(qi, n, gates, theta, terms, ps_ids, (np.pi / 2, -np.pi / 2), stream))
@@ -451,6 +453,84 @@ def per_gate_leg(qi, workloads, stream, n, peak):
     return out
 
 
+def costmodel_eval(qi, workloads, torch, np, n_train=28, count=4000, qubits=range(28, 35), exhaustive_upto=30):
+    """The learned-fusion configuration: the cost model trained on `count` engine-timed blocks
+    at n_train qubits, then seeded random circuits of the benchmark family (one per qubit count
+    in `qubits`, depth 20-60) planned three ways — greedy fixed-k, the learned choice, and (up to
+    `exhaustive_upto` qubits) exhaustive timing of every preset partition — with measured wall
+    time as the judge, and the learned plan's infidelity against the FP64 per-gate path up to
+    33 qubits (FP64 at 34 qubits would need 256 GiB)."""
+    from quant_iron_gb300 import costmodel
+    t0 = time.perf_counter()
+    X, y = costmodel.collect(n_train, count, seed=11)
+    t_collect = time.perf_counter() - t0
+    idx = np.random.default_rng(0).permutation(len(y))
+    cut = int(0.9 * len(y))
+    hist = costmodel.train(X[idx[:cut]], y[idx[:cut]], epochs=2000, lr=3e-3, seed=1)
+    pred = costmodel.predict(X[idx[cut:]])
+    out = {"training": {"qubits": n_train, "timings": int(count), "collect_s": t_collect,
+                        "loss_first": float(hist[0]), "loss_last": float(hist[-1]),
+                        "holdout_corr": float(np.corrcoef(pred, y[idx[cut:]])[0, 1]),
+                        "holdout_rmse_log_ms": float(np.sqrt(np.mean((pred - y[idx[cut:]]) ** 2)))},
+           "circuits": []}
+
+    def timed(plan, st, reps=2):
+        st.set_plus()
+        plan.execute(st)
+        st.synchronize()
+        best = 1e30
+        for _ in range(reps):
+            st.set_plus()
+            st.synchronize()
+            t1 = time.perf_counter()
+            plan.execute(st)
+            st.synchronize()
+            best = min(best, time.perf_counter() - t1)
+        return best * 1e3
+
+    for n in qubits:
+        depth = 20 + (7 * n) % 41
+        gates = workloads.random_circuit(n, depth, seed=100 + n)
+        st = qi.DeviceState(n, qi.F32)
+        rec = {"qubits": n, "layers": depth, "gates": int(gates.size)}
+        pg = qi.Plan(n, qi.F32, gates, fusion=qi.FUSION_GREEDY, max_block_qubits=6)
+        rec["greedy_ms"] = timed(pg, st)
+        t1 = time.perf_counter()
+        pl = qi.Plan(n, qi.F32, gates, fusion=qi.FUSION_LEARNED, max_block_qubits=6)
+        rec["learned_plan_build_s"] = time.perf_counter() - t1
+        rec["learned_ms"] = timed(pl, st)
+        rec["learned_predicted_ms"] = pl.stats()["predicted_us"] / 1e3
+        rec["learned_kernels"] = pl.stats()["n_kernels"]
+        rec["greedy_kernels"] = pg.stats()["n_kernels"]
+        if n <= exhaustive_upto:
+            ex = {}
+            for k in (2, 3, 4, 5, 6):
+                for tc in ((0, 2) if k >= 5 else (2,)):
+                    ex["k%d%s" % (k, "_tc" if tc == 0 else "")] = timed(
+                        qi.Plan(n, qi.F32, gates, fusion=qi.FUSION_GREEDY, max_block_qubits=k, use_tensor_cores=tc), st)
+            ex["per_gate"] = timed(qi.Plan(n, qi.F32, gates, fusion=qi.FUSION_NONE), st, reps=1)
+            rec["exhaustive_ms"] = ex
+            rec["exhaustive_best"] = min(ex, key=ex.get)
+            rec["exhaustive_best_ms"] = ex[rec["exhaustive_best"]]
+        if n <= 33:
+            s64 = qi.DeviceState(n, qi.F64)
+            s64.set_plus()
+            qi.Plan(n, qi.F64, gates, fusion=qi.FUSION_NONE).execute(s64)
+            st.set_plus()
+            pl.execute(st)
+            rec["learned_infidelity"] = st.compare(s64)["infidelity"]
+            s64.close()
+        st.close()
+        out["circuits"].append(rec)
+        print(json.dumps(rec), file=sys.stderr, flush=True)
+    c = out["circuits"]
+    out["summary"] = {"learned_over_greedy_wall": [x["learned_ms"] / x["greedy_ms"] for x in c],
+                      "learned_over_exhaustive_best": [x["learned_ms"] / x["exhaustive_best_ms"] for x in c
+                                                       if "exhaustive_best_ms" in x],
+                      "max_infidelity": max(x.get("learned_infidelity", 0.0) for x in c)}
+    return out
+
+
 def run_reference(args):
     """The reference implementation's CPU path (the oracle port of its rayon data flow; the
     crate itself needs a Rust toolchain, absent on both machines) on this workload.  A step
@@ -574,6 +654,12 @@ def main():
     from quant_iron_gb300 import workloads
     qi._abi.check(qi._abi.lib.qi_set_device(local))
 
+    if args.costmodel_eval:
+        print(json.dumps(costmodel_eval(qi, workloads, torch, np)))
+        return
+    if args.adjoint_fd == "all":   # the adjoint configuration alone, every parameter checked
+        print(json.dumps(adjoint_leg(qi, workloads, torch.cuda.Stream(), torch, np, fd="all")))
+        return
     n = args.qubits
     gates = workloads.random_circuit(n, LAYERS, seed=SEED)
     terms = workloads.heisenberg_open_chain(n, seed=SEED)
@@ -649,13 +735,13 @@ def main():
         # here by the engine's own probe kernel (MEASURED_PEAKS.json holds no TF32 figure)
         probe_clk = ClockSampler(local)
         probe_clk.start()
-        tf32_peak, probe_ms = qi.tf32_rate_probe(iters=16384, reps=5)
+        tf32_peak, probe_ms = qi.tf32_rate_probe(iters=65536, reps=40)   # ~0.2 s: clocks sampled under load
         pclk = probe_clk.stop()
         tflop = 3 * 8 * (1 << FUSED_K) * (1 << n) / 1e12
         roofline["tensor"] = {"achieved": tflop / (avg_ms / 1e3), "peak": tf32_peak, "unit": "TFLOP/s",
                               "frac": tflop / (avg_ms / 1e3) / tf32_peak,
                               "peak_source": "measured here: qi_tf32_rate_probe (tcgen05.mma kind::tf32 M128 N256 "
-                                             "K8, one CTA per SM, best of 5 launches of %.2f ms)" % probe_ms,
+                                             "K8, one CTA per SM, best of 40 launches of %.2f ms)" % probe_ms,
                               "peak_clocks": pclk, "flop_per_amp": 3 * 8 * (1 << FUSED_K)}
 
     # energy of the final state (FP64 reduction), and the time of SumOp::expectation_value
@@ -698,7 +784,7 @@ def main():
                                       "energy_error": max(x["energy_error"] for x in seeds),
                                       "speedup": min(x["speedup"] for x in seeds)}}
         extra["per_gate"] = per_gate_leg(qi, workloads, stream, n, peak)
-        extra["adjoint"] = adjoint_leg(qi, workloads, stream, torch, np, fd=args.adjoint_fd)
+        extra["adjoint"] = adjoint_leg(qi, workloads, stream, torch, np)
         extra["trotter"] = trotter_leg(qi, workloads, stream, torch, np)
     extra["expectation"] = expectation
 
@@ -723,6 +809,19 @@ def main():
                 s2.upload_async(host_in.data_ptr(), dim)   # the device, so none may happen in the timed loop)
                 plan.execute(s2)
                 s2.synchronize()
+            # the host link on its own (copy engine, page-locked buffers): what the pipeline hides
+            link = {}
+            for name, fn in (("h2d_ms", lambda: st.upload_async(host_in.data_ptr(), dim)),
+                             ("d2h_ms", lambda: st.download_async(host_out[0].data_ptr(), dim))):
+                torch.cuda.synchronize()
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                fn()
+                b.record(stream)
+                torch.cuda.synchronize()
+                link[name] = a.elapsed_time(b)
+            link["h2d_gbs"] = 16 * dim / (link["h2d_ms"] / 1e3) / 1e9
+            link["d2h_gbs"] = 16 * dim / (link["d2h_ms"] / 1e3) / 1e9
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         e0 = torch.cuda.Event(enable_timing=True)
@@ -733,12 +832,16 @@ def main():
             # download), so each runs at the full device rate while the other state's download and
             # next upload use the copy engines
             e2e_steps = max(2, args.steps)
+            circuit_end = []
             for k in range(e2e_steps):
                 s2, other = states[k % 2], states[(k + 1) % 2]
                 s2.upload_async(host_in.data_ptr(), dim)
                 if k > 0:
                     s2.wait_for(other)   # other's stream so far ends with its circuit
                 plan.execute(s2)
+                ce = torch.cuda.Event(enable_timing=True)
+                ce.record(stream if k % 2 == 0 else stream2)
+                circuit_end.append(ce)
                 if k > 0:
                     other.download_async(host_out[(k - 1) % 2].data_ptr(), dim)
             states[(e2e_steps - 1) % 2].download_async(host_out[(e2e_steps - 1) % 2].data_ptr(), dim)
@@ -761,6 +864,10 @@ def main():
                             "copy engines overlap the other state's circuit" if pipelined
                             else "one state, transfers in order")}
         if pipelined:
+            ends = [e0.elapsed_time(c) for c in circuit_end]
+            e2e["link"] = link
+            e2e["circuit_end_ms"] = [round(x, 1) for x in ends]
+            e2e["steady_ms_per_step"] = (ends[-1] - ends[0]) / max(1, len(ends) - 1)
             st2.close()
             del host_out
         del host_in

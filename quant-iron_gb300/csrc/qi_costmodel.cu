@@ -2,10 +2,13 @@
 // own timing collection that trains the learned cost model (qi_mlp.cu).
 //
 // QI_FUSION_GREEDY uses the greedy fixed-k fuser (window_partition, qi_plan.cu).
-// QI_FUSION_LEARNED builds the candidate partitions {one kernel per gate} and
-// {greedy k, tensor cores on/off} for k = 2..kmax, predicts every device op's time with the trained
-// MLP, and keeps the candidate with the smallest predicted sum; without a
-// trained model it falls back to greedy.
+// QI_FUSION_LEARNED scores partitions with the trained MLP in two ways and keeps the plan with the
+// smallest predicted device time: (1) whole-plan candidates {one kernel per gate} and {greedy k,
+// tensor cores on/off} for k = 2..kmax; (2) a partition built block by block, where each step
+// scores the greedy fuser's own candidate blocks — the first remaining gate's light-cone block and
+// everything each window of w consecutive qubits can absorb, for every w = 2..kmax — and takes the
+// block that saves the most predicted time against running its gates one kernel each (which
+// gates merge, and at what k).  Without a trained model it falls back to greedy.
 #include "qi_plan.hpp"
 #include "qi_mlp.hpp"
 
@@ -16,7 +19,132 @@
 
 namespace qi {
 
+// Features of the device op a block lowers to (per-gate kernel, diagonal table, dense block on
+// the tensor or the CUDA cores), as build_plan lowers it.
+static void block_features(int n, bool f32, bool tc, const std::vector<Elem> &elems, const Block &b, float *f) {
+    if (b.single) {
+        const Elem &e = elems[b.members[0]];
+        int t[6] = {0, 0, 0, 0, 0, 0}, kk = 0, nc = 0, shape = CS_GENERAL;
+        if (e.pauli) {
+            const uint64_t m = e.gm.xmask | e.gm.zmask;
+            for (int q = 0; q < 64 && kk < 6; ++q)
+                if ((m >> q) & 1ull) t[kk++] = q;
+            shape = e.gm.xmask ? CS_GENERAL : CS_DIAGONAL;
+        } else if (e.gm.nt > 0) {
+            for (int j = 0; j < e.gm.nt; ++j) t[kk++] = e.gm.t[j];
+            nc = (int)e.gm.controls.size();
+            const Op op = lower_gate(n, e.gm);
+            shape = per_gate_shape(op.kind, op.mode);
+        }
+        op_features(n, f32, CC_PER_GATE, kk, t, nc, shape, f);
+        return;
+    }
+    bool diag = true;
+    for (int idx : b.members) diag = diag && elems[idx].diagonal;
+    int t[6] = {0, 0, 0, 0, 0, 0}, kk = 0;
+    for (int q = 0; q < 64 && kk < 6; ++q)
+        if ((b.mask >> q) & 1ull) t[kk++] = q;
+    int cls = CC_DENSE_SIMT;
+    if (diag) cls = CC_DIAG;
+    else if (tc && f32 && kk >= 5 && n >= kk + 7) cls = CC_DENSE_TC;
+    op_features(n, f32, cls, kk, t, 0, diag ? CS_DIAGONAL : CS_GENERAL, f);
+}
+
+// Predicted ms of each feature row (caller holds the model's mutex).
+static bool predict_ms(Mlp &m, int n, const std::vector<float> &F, std::vector<double> &ms) {
+    const int rows = (int)(F.size() / kFeat);
+    ms.assign((size_t)rows, 0.0);
+    if (rows == 0) return true;
+    std::vector<float> y((size_t)rows);
+    Status s = m.ensure_device(rows);
+    if (s.ok()) s = m.upload_params(nullptr);
+    if (s.ok()) s = m.predict(F.data(), rows, y.data(), nullptr);
+    if (!s.ok()) return false;
+    for (int i = 0; i < rows; ++i) ms[(size_t)i] = ms_from_y(y[(size_t)i], n);
+    return true;
+}
+
+// The model-scored partition (see the file comment); empty on failure.  Caller holds m.mu.
+static std::vector<Block> learned_partition_locked(Mlp &m, int n, bool f32, bool tc, const std::vector<Elem> &elems,
+                                                   int kmax, double *pred_ms) {
+    std::vector<Block> blocks;
+    // every gate as its own kernel: the baseline a block's saving is measured against
+    std::vector<float> F((size_t)elems.size() * kFeat);
+    for (size_t i = 0; i < elems.size(); ++i) {
+        Block one;
+        one.members.push_back((int)i);
+        one.mask = elems[i].mask;
+        one.single = true;
+        block_features(n, f32, tc, elems, one, F.data() + i * kFeat);
+    }
+    std::vector<double> t_gate;
+    if (!predict_ms(m, n, F, t_gate)) return {};
+    std::vector<int> remaining(elems.size());
+    for (size_t i = 0; i < elems.size(); ++i) remaining[i] = (int)i;
+    std::vector<char> taken(elems.size(), 0);
+    double total = 0.0;
+    std::vector<Block> cands;
+    std::vector<double> t_cand;
+    while (!remaining.empty()) {
+        cands.clear();
+        Block lc = light_cone_block(elems, remaining, n, kmax);
+        bool diag = !lc.single;
+        for (int idx : lc.members) diag = diag && elems[idx].diagonal;
+        const bool alone = lc.single || diag;   // a lone gate, or a diagonal block for a phase-polynomial run
+        cands.push_back(std::move(lc));
+        if (!alone) {
+            for (int w = 2; w <= kmax; ++w) {
+                const uint64_t win = (1ull << w) - 1;
+                for (int a = 0; a + w <= n; ++a) {
+                    Block b = window_block(elems, remaining, win << a);
+                    if (b.members.size() >= 2) cands.push_back(std::move(b));
+                }
+            }
+        }
+        size_t best = 0;
+        if (cands.size() > 1) {
+            F.assign(cands.size() * kFeat, 0.0f);
+            for (size_t c = 0; c < cands.size(); ++c) block_features(n, f32, tc, elems, cands[c], F.data() + c * kFeat);
+            if (!predict_ms(m, n, F, t_cand)) return {};
+            double best_save = -1e300;
+            for (size_t c = 0; c < cands.size(); ++c) {
+                double per_gate = 0.0;
+                for (int idx : cands[c].members) per_gate += t_gate[(size_t)idx];
+                const double save = per_gate - t_cand[c];
+                if (save > best_save || (save == best_save && cands[c].members.size() > cands[best].members.size())) {
+                    best_save = save;
+                    best = c;
+                }
+            }
+            total += t_cand[best];
+        } else {
+            double per_gate = 0.0;
+            for (int idx : cands[0].members) per_gate += t_gate[(size_t)idx];
+            total += cands[0].single ? per_gate : per_gate * 0.25;   // diagonal runs share one pass
+        }
+        Block b = std::move(cands[best]);
+        for (int idx : b.members) taken[(size_t)idx] = 1;
+        std::vector<int> rest;
+        rest.reserve(remaining.size());
+        for (int idx : remaining)
+            if (!taken[(size_t)idx]) rest.push_back(idx);
+        remaining.swap(rest);
+        blocks.push_back(std::move(b));
+    }
+    if (pred_ms) *pred_ms = total;
+    return blocks;
+}
+
 std::vector<Block> choose_partition(qi_plan *p, const std::vector<Elem> &elems, int kmax) {
+    if (p->learned_blocks) {
+        Mlp &m = global_mlp();
+        std::lock_guard<std::mutex> lk(m.mu);
+        if (m.trained) {
+            std::vector<Block> b = learned_partition_locked(m, p->n, p->prec == QI_F32,
+                                                            p->opts.use_tensor_cores != 2, elems, kmax, nullptr);
+            if (!b.empty() || elems.empty()) return b;
+        }
+    }
     return window_partition(elems, p->n, kmax);
 }
 
@@ -103,6 +231,28 @@ bool learned_choice(qi_plan *p, const std::vector<Elem> &elems, int kmax, int *k
         for (int i = 0; i < c.count; ++i) ms += ms_from_y(y[(size_t)(c.first + i)], n);
         ms += c.nnorm * 1.5 * ms_from_y(y[(size_t)norm_row], n);
         if (ms < best) { best = ms; bk = c.k; btc = c.tc; }
+    }
+    // the block-by-block partition at kmax, tensor cores as the caller allows
+    p->learned_blocks = false;
+    const bool tc_ok = p->opts.use_tensor_cores != 2;
+    double lp_ms = 0.0;
+    const std::vector<Block> lp = learned_partition_locked(m, n, f32, tc_ok, elems, kmax, &lp_ms);
+    if (!lp.empty()) {
+        bool any_tc = false;
+        for (const Block &b : lp) {
+            if (b.single) continue;
+            bool diag = true;
+            for (int idx : b.members) diag = diag && elems[idx].diagonal;
+            const int w = __builtin_popcountll(b.mask);
+            any_tc = any_tc || (!diag && tc_ok && f32 && w >= 5 && n >= w + 7);
+        }
+        lp_ms += (any_tc ? 1.5 : 0.0) * ms_from_y(y[(size_t)norm_row], n);
+        if (lp_ms < best) {
+            best = lp_ms;
+            bk = kmax;
+            btc = tc_ok ? 1 : 0;
+            p->learned_blocks = true;
+        }
     }
     *k_out = bk;
     *tc_out = btc;

@@ -147,7 +147,7 @@ static void left_multiply(std::vector<cd> &B, int nq, const std::vector<int> &po
 // The light-cone block of the first remaining element: scan the remaining
 // elements in order, absorbing every one that fits (|Q u S| <= k) and depends
 // on no passed-over element.
-static Block light_cone_block(const std::vector<Elem> &elems, const std::vector<int> &remaining, int n, int kmax) {
+Block light_cone_block(const std::vector<Elem> &elems, const std::vector<int> &remaining, int n, int kmax) {
     Block b;
     const uint64_t all = n >= 64 ? ~0ull : ((1ull << n) - 1);
     const Elem &first = elems[remaining[0]];
@@ -183,7 +183,7 @@ static Block light_cone_block(const std::vector<Elem> &elems, const std::vector<
 
 // Everything the window W can absorb: the remaining elements on qubits inside W
 // that depend on no passed-over element (same blocking rule as above).
-static Block window_block(const std::vector<Elem> &elems, const std::vector<int> &remaining, uint64_t W) {
+Block window_block(const std::vector<Elem> &elems, const std::vector<int> &remaining, uint64_t W) {
     Block b;
     uint64_t blocked_any = 0, blocked_diag = 0;
     for (int idx : remaining) {

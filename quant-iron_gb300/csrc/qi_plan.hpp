@@ -30,6 +30,10 @@ std::vector<Block> greedy_partition(const std::vector<Elem> &elems, int n, int k
 // (taken as is when it is all-diagonal), and everything each window of kmax
 // consecutive qubits can absorb; the candidate with the most elements wins.
 std::vector<Block> window_partition(const std::vector<Elem> &elems, int n, int kmax);
+// The light-cone block of the first remaining element (at most kmax qubits), and everything the
+// qubit window W can absorb from the remaining elements (order and commutation respected).
+Block light_cone_block(const std::vector<Elem> &elems, const std::vector<int> &remaining, int n, int kmax);
+Block window_block(const std::vector<Elem> &elems, const std::vector<int> &remaining, uint64_t W);
 void compose_block(const std::vector<Elem> &elems, const Block &b, std::vector<int> &qubits,
                    std::vector<std::complex<double>> &B);
 
@@ -48,6 +52,7 @@ struct qi_plan {
     std::vector<qi::PhasePoly> polys;         // host copy of each OP_PHASE_POLY op (op.mat_offset indexes it)
     qi_plan_stats stats = {};
     std::vector<qi::Block> partition_override;   // set by callers that chose the partition
+    bool learned_blocks = false;                 // QI_FUSION_LEARNED chose the model-scored partition
 };
 
 namespace qi {

@@ -3,7 +3,9 @@
 CPU: the FP64 MLP oracle's gradient against central differences; the feature
 layout constants.  GPU: the engine's hand-written training kernels against the
 FP64 oracle; training on engine-measured timings; and what the trained model
-gains over the method without it (greedy fixed-k fusion) in measured wall time.
+gains over the method without it (greedy fixed-k fusion) in measured wall time:
+in FP64 (where dense blocks are FP64-bound and the model turns fusion down) and
+in FP32 (where it scores the fuser's candidate blocks).
 """
 import os
 import sys
@@ -86,8 +88,11 @@ def test_train_on_engine_timings_and_learned_gain():
     assert st64["predicted_us"] > 0
     assert t_learned64 < 0.8 * t_greedy64, (t_learned64, t_greedy64)
     assert t_learned64 < 1.5 * min(t_none64, t_greedy64), (t_learned64, t_none64, t_greedy64)
-    # FP32: the learned choice is within 50% of the best measured candidate
-    cands = [wall(qi.F32, fusion=qi.FUSION_GREEDY, max_block_qubits=k)[0] for k in (3, 4, 5, 6)]
-    cands.append(wall(qi.F32, fusion=qi.FUSION_NONE)[0])
-    t_learned32, _ = wall(qi.F32, fusion=qi.FUSION_LEARNED)
-    assert t_learned32 < 1.5 * min(cands), (t_learned32, cands)
+    # FP32: the model-scored plan (block by block, or a whole-plan preset, whichever it predicts
+    # faster) is no slower than the greedy fixed-k fuser it falls back to (5% for timing noise)
+    t_greedy32, _ = wall(qi.F32, fusion=qi.FUSION_GREEDY, max_block_qubits=6)
+    t_learned32, st32 = wall(qi.F32, fusion=qi.FUSION_LEARNED, max_block_qubits=6)
+    assert st32["predicted_us"] > 0
+    print("FP32 greedy %.3f ms, learned %.3f ms (%d kernels), gain %.1f%%" %
+          (t_greedy32 * 1e3, t_learned32 * 1e3, st32["n_kernels"], 100 * (1 - t_learned32 / t_greedy32)))
+    assert t_learned32 <= 1.05 * t_greedy32, (t_learned32, t_greedy32)

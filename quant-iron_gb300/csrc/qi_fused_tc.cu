@@ -49,7 +49,6 @@
 #include <algorithm>
 #include <atomic>
 #include <cmath>
-#include <cstdlib>
 
 namespace qi {
 
@@ -260,31 +259,23 @@ __device__ __forceinline__ bool warp_wait_or_abort(uint64_t *bar, uint32_t parit
 constexpr int kPhaseLane = 64, kPhaseTile = 64 + 128 * 8;
 
 // ------------------------------------------------------------------ kernel
-// Tile loading: whole tiles (TL_TILE), tile pairs through a ring of 8-row units of both tiles
-// (TL_PAIR), or single tiles through a ring of 8-row units released as soon as they are read
-// (TL_UNIT).
-enum TileLoad : int { TL_TILE = 0, TL_PAIR = 1, TL_UNIT = 2 };
-template <int K, int MODE = TL_TILE>
+template <int K, bool PAIR = false>
 struct TcCfg {
-    static constexpr bool PAIR = MODE == TL_PAIR, RING = MODE != TL_TILE;
     static constexpr int R = 1 << K;                   // rows (target patterns)
     static constexpr int BLK = R * R;                  // floats per operand block
     static constexpr uint32_t LBO = 128;               // next core matrix along K
     static constexpr uint32_t SBO = (R / 4) * 128;     // next 8-row group along N
-    // shared buffers: whole tiles, or a ring of 8-row units (pair mode: 2 KB rows of both tiles)
-    static constexpr int NBUF = MODE == TL_PAIR ? 10 : MODE == TL_UNIT ? 16 : (K == 6 ? 2 : 6);
+    // shared buffers: whole tiles, or (pair mode) a ring of units of 16 rows x 2 KB runs
+    static constexpr int NBUF = PAIR ? 10 : (K == 6 ? 2 : 6);
     static constexpr uint32_t STAGE = 2 * R;           // TMEM columns of one A stage or one accumulator
     static constexpr uint32_t COL_A = 0, COL_D = 2 * STAGE;
     static constexpr uint32_t TMEM_COLS = 4 * STAGE;   // 512 for k = 6, 256 for k = 5
     static constexpr int CONV_ROWS = R / 2;            // rows per converter thread (2 row slices)
-    static constexpr int CHUNK = RING ? 8 : 16;        // rows converted per step (register footprint)
+    static constexpr int CHUNK = PAIR ? 8 : 16;        // rows converted per step (register footprint)
     static constexpr uint32_t TILE_BYTES = (uint32_t)R * 128 * sizeof(float2);
     static constexpr int UNIT_ROWS = 8;                // pair mode: rows per ring unit (one chunk)
     static constexpr int UNITS_PER_PAIR = 2 * CONV_ROWS / UNIT_ROWS;   // pair mode: 8
-    static constexpr int UNITS_PER_TILE = 2 * CONV_ROWS / UNIT_ROWS;   // unit mode: 8
-    static constexpr uint32_t BUF_BYTES = PAIR   ? (uint32_t)UNIT_ROWS * 2 * 128 * sizeof(float2)
-                                          : RING ? (uint32_t)UNIT_ROWS * 128 * sizeof(float2)
-                                                 : TILE_BYTES;
+    static constexpr uint32_t BUF_BYTES = PAIR ? (uint32_t)UNIT_ROWS * 2 * 128 * sizeof(float2) : TILE_BYTES;
     // operand blocks in shared memory: -Im U, Re U, Im U (hi, then lo); pair mode Re U, Im U
     static constexpr int NBLK = PAIR ? 4 : 6;
     static constexpr size_t OFF_TILES = (size_t)NBLK * BLK * sizeof(float);
@@ -364,14 +355,13 @@ __device__ __forceinline__ void st_cs_v8(float2 *p, float a0, float a1, float a2
 // chunk's row pairs starting at its own (lane mod 8), undone in registers.
 // PHASE: a diagonal phase polynomial exp(2 pi i f(x)) that follows the block in the plan is
 // applied by the epilogue before the store (its phase table at `poly`, tc_phase_table).
-template <int K, int MODE, bool ROT, bool PHASE>
+template <int K, bool PAIR, bool ROT, bool PHASE>
 __global__ void __launch_bounds__(kTcThreads, 1) k_fused_tc(float2 *a, const float *blocks, TileGeom g, int *err_flag,
                                                             const uint32_t *__restrict__ poly) {
-    using C = TcCfg<K, MODE>;
-    constexpr bool PAIR = C::PAIR, RING = C::RING;
+    using C = TcCfg<K, PAIR>;
     constexpr int R = C::R, NB = C::NBUF;
-    static_assert(!RING || (K == 6 && C::UNIT_ROWS == C::CHUNK), "unit rings: K = 6, one ring unit per chunk");
-    static_assert(!(RING && ROT), "ring-mode tiles have qubit 0 as a column");
+    static_assert(!PAIR || (K == 6 && C::UNIT_ROWS == C::CHUNK), "pair mode: K = 6, one ring unit per chunk");
+    static_assert(!(PAIR && ROT), "pair-mode tiles have qubit 0 as a column");
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     float *sB = reinterpret_cast<float *>(smem_raw);   // operand blocks (C::NBLK)
     unsigned char *tiles = smem_raw + C::OFF_TILES;
@@ -411,8 +401,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_fused_tc(float2 *a, const flo
             const uint32_t bit = ((uint32_t)tid >> (g.nlow_t + j)) & 1u;
             // pair mode: the top row bits select the ring unit (slice, chunk); the others index
             // its runs of 2 x 2^L
-            if (!RING) x |= bit << (g.L + j);
-            else if ((1 << j) < C::UNIT_ROWS) x |= bit << (g.L + (PAIR ? 1 : 0) + j);
+            if (!PAIR) x |= bit << (g.L + j);
+            else if ((1 << j) < C::UNIT_ROWS) x |= bit << (g.L + 1 + j);
             go |= (uint64_t)bit << g.high_t[j];
         }
         rowx[tid] = x;
@@ -421,7 +411,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_fused_tc(float2 *a, const flo
     if (tid == 0) {
         for (int i = 0; i < NB; ++i) {
             mbar_init(raw_full + i, 1);
-            mbar_init(raw_empty + i, RING ? kConvWarps / 2 : kConvWarps);   // ring units: one slice per unit
+            mbar_init(raw_empty + i, PAIR ? kConvWarps / 2 : kConvWarps);   // pair mode: one slice per unit
         }
         for (int i = 0; i < 2; ++i) {
             mbar_init(a_full + i, kConvWarps);
@@ -457,7 +447,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_fused_tc(float2 *a, const flo
         const int r0 = slice * C::CONV_ROWS;
         for (int it = 0; tile_of(it) < ntiles; ++it) {
             const int b = it % NB;   // whole-tile buffer (pair mode: units, below)
-            if (!RING && !warp_wait_or_abort(raw_full + b, (uint32_t)(it / NB) & 1u, abort_flag, err_flag)) break;
+            if (!PAIR && !warp_wait_or_abort(raw_full + b, (uint32_t)(it / NB) & 1u, abort_flag, err_flag)) break;
             // real half -> A stage 0, once the products of the previous tile have read it;
             // the imaginary parts stay in registers for stage 1
             if (it > 0 && !warp_wait_or_abort(a_empty + 0, (uint32_t)(it - 1) & 1u, abort_flag, err_flag)) break;
@@ -477,15 +467,6 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_fused_tc(float2 *a, const flo
                         break;
                     }
                     S = reinterpret_cast<const float2 *>(tiles + (size_t)unit * C::BUF_BYTES) + ((uint32_t)(it & 1) << g.L);
-                } else if constexpr (RING) {   // unit k of this CTA's sequence: tile it, chunk c0, slice
-                    const uint32_t k = (uint32_t)C::UNITS_PER_TILE * (uint32_t)it + 2u * (uint32_t)(c0 / C::CHUNK) +
-                                       (uint32_t)slice;
-                    unit = k % NB;
-                    if (!warp_wait_or_abort(raw_full + unit, (k / NB) & 1u, abort_flag, err_flag)) {
-                        ok = false;
-                        break;
-                    }
-                    S = reinterpret_cast<const float2 *>(tiles + (size_t)unit * C::BUF_BYTES);
                 } else {
                     S = reinterpret_cast<const float2 *>(tiles + (size_t)b * C::BUF_BYTES);
                 }
@@ -532,10 +513,6 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_fused_tc(float2 *a, const flo
                         im[c0 + i] = v.y;
                     }
                 }
-                if constexpr (RING && !PAIR) {   // the chunk is in registers: the unit may take new rows
-                    __syncwarp();
-                    if (lane == 0) mbar_arrive(raw_empty + unit);
-                }
                 split_store<C::CHUNK>(tmem + lane_base + C::COL_A + r0 + c0, tmem + lane_base + C::COL_A + R + r0 + c0,
                                       re);
                 if constexpr (PAIR) {   // the pair's second tile was the unit's last reader
@@ -544,7 +521,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_fused_tc(float2 *a, const flo
                 }
             }
             if (!ok) break;
-            if (!RING) {
+            if (!PAIR) {
                 __syncwarp();
                 if (lane == 0) mbar_arrive(raw_empty + b);   // the buffer may take the next tile
             }
@@ -653,32 +630,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_fused_tc(float2 *a, const flo
         // ------------------------------------------------ producer (one thread)
         if (lane == 0) {
             const uint32_t run_bytes = (uint32_t)sizeof(float2) << g.L;
-            if constexpr (MODE == TL_UNIT) {
-                // unit k = 8 it + u (u = 2c + s) <- rows 32 s + 8 c .. + 7 of tile it, in the order
-                // the converters read them
-                int issued = 0;
-                bool ok = true;
-                for (int it = 0; ok && tile_of(it) < ntiles; ++it) {
-                    const uint64_t base = tile_base(g, tile_of(it));
-                    for (uint32_t u = 0; u < (uint32_t)C::UNITS_PER_TILE; ++u) {
-                        const uint32_t k = (uint32_t)C::UNITS_PER_TILE * (uint32_t)it + u, unit = k % NB;
-                        if (k >= (uint32_t)NB &&
-                            !wait_or_abort(raw_empty + unit, (k / NB - 1) & 1u, abort_flag, err_flag)) {
-                            ok = false;
-                            break;
-                        }
-                        mbar_arrive_expect_tx(raw_full + unit, C::BUF_BYTES);
-                        unsigned char *dst = tiles + (size_t)unit * C::BUF_BYTES;
-                        const int row0 = 32 * (int)(u & 1u) + C::UNIT_ROWS * (int)(u >> 1);
-                        for (int i = 0; i < C::UNIT_ROWS; ++i)
-                            bulk_load(dst + (size_t)i * run_bytes, a + (base | grow[row0 + i]), run_bytes, raw_full + unit);
-                        issued = (int)k + 1;
-                    }
-                }
-                // copies still in flight (only after an abort) land before the CTA exits
-                for (int j = issued > NB ? issued - NB : 0; j < issued; ++j)
-                    if (!mbar_wait_bounded(raw_full + (j % NB), (uint32_t)(j / NB) & 1u)) atomicExch(err_flag, 2);
-            } else if (!PAIR) {
+            if (!PAIR) {
                 const int nruns = 1 << g.nhigh;
                 int issued = 0;
                 for (int it = 0; tile_of(it) < ntiles; ++it) {
@@ -904,10 +856,9 @@ bool tc_phase_table(const PhasePoly &pp, int k, const int32_t *targets, std::vec
     return true;
 }
 
-template <int K, int MODE, bool ROT, bool PHASE>
+template <int K, bool PAIR, bool ROT, bool PHASE>
 static Status launch_tc_t(qi_state *s, const TileGeom &g, const void *d_tc, const void *poly) {
-    using C = TcCfg<K, MODE>;
-    constexpr bool PAIR = C::PAIR;
+    using C = TcCfg<K, PAIR>;
     static_assert(C::SMEM <= 232448, "shared memory per CTA");
     // the shared-memory opt-in and the SM count are per device (state handles may live on several)
     static std::atomic<int> num_sms_of[64];
@@ -916,14 +867,14 @@ static Status launch_tc_t(qi_state *s, const TileGeom &g, const void *d_tc, cons
     if (dev < 0 || dev >= 64) return err(QI_ERR_UNSUPPORTED, dev, 64, "device ordinal");
     int num_sms = num_sms_of[dev].load();
     if (num_sms == 0) {
-        QI_CUDA(cudaFuncSetAttribute(k_fused_tc<K, MODE, ROT, PHASE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        QI_CUDA(cudaFuncSetAttribute(k_fused_tc<K, PAIR, ROT, PHASE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)C::SMEM));
         QI_CUDA(cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, dev));
         num_sms_of[dev].store(num_sms);
     }
     uint64_t grid = PAIR ? g.ntiles / 2 : g.ntiles;   // one persistent CTA per SM
     if (grid > (uint64_t)num_sms) grid = (uint64_t)num_sms;
-    k_fused_tc<K, MODE, ROT, PHASE><<<(unsigned)grid, kTcThreads, C::SMEM, s->stream>>>(
+    k_fused_tc<K, PAIR, ROT, PHASE><<<(unsigned)grid, kTcThreads, C::SMEM, s->stream>>>(
         (float2 *)s->amps, (const float *)d_tc, g, s->d_flag, (const uint32_t *)poly);
     count_launch();
     return check_launch("k_fused_tc");
@@ -947,16 +898,9 @@ Status launch_fused_tc(qi_state *s, int k, const int32_t *targets, const void *d
     if (poly && ((uintptr_t)poly & 15) != 0) return err(QI_ERR_UNKNOWN, -1, -1, "phase block must be 16-byte aligned");
 #define QI_TC(KK, PA, RO)                                                                    \
     (poly ? launch_tc_t<KK, PA, RO, true>(s, g, d_tc, poly) : launch_tc_t<KK, PA, RO, false>(s, g, d_tc, nullptr))
-    if (k == 5) return rot ? QI_TC(5, TL_TILE, true) : QI_TC(5, TL_TILE, false);
-    if (pair) {
-        static const int ring_mode = [] {
-            const char *v = std::getenv("QI_TC_RING");
-            return (v && v[0] == 'u') ? (int)TL_UNIT : (int)TL_PAIR;
-        }();
-        if (ring_mode == TL_UNIT) return QI_TC(6, TL_UNIT, false);
-        return QI_TC(6, TL_PAIR, false);
-    }
-    return rot ? QI_TC(6, TL_TILE, true) : QI_TC(6, TL_TILE, false);
+    if (k == 5) return rot ? QI_TC(5, false, true) : QI_TC(5, false, false);
+    if (pair) return QI_TC(6, true, false);
+    return rot ? QI_TC(6, false, true) : QI_TC(6, false, false);
 #undef QI_TC
 }
 

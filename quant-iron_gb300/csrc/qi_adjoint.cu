@@ -609,23 +609,49 @@ static std::vector<SweepStep> plan_reverse_sweep(const std::vector<GateMatrix> &
         return !m.pauli && m.nt == 1 && m.controls.empty() && n_params(jj) <= 1;
     };
     const int max_q = f32 ? kMultiQubits : kMultiQubits - 1;   // FP64 x 16 amplitudes spills
-    std::vector<SweepStep> steps;
-    for (int64_t j = n_gates - 1; j >= 0;) {
+    // One group from gate j down, at most `limit` qubits; returns the gate below it.
+    auto take_group = [&](int64_t j, int limit, int *nq) {
         int qcount[64] = {0};
         uint64_t qmask = 0;
         int64_t jj = j;
         for (; jj >= 0 && groupable(jj); --jj) {
             const int q = mats[(size_t)jj].t[0];
-            if (!((qmask >> q) & 1ull) && __builtin_popcountll(qmask) == max_q) break;
+            if (!((qmask >> q) & 1ull) && __builtin_popcountll(qmask) == limit) break;
             if (qcount[q] == kMultiStages) break;
             qmask |= 1ull << q;
             ++qcount[q];
         }
+        if (nq) *nq = __builtin_popcountll(qmask);
+        return jj;
+    };
+    std::vector<SweepStep> steps;
+    bool in_run = false;   // the previous pass was a group ending where this one starts
+    for (int64_t j = n_gates - 1; j >= 0;) {
+        // At the start of a run of groupable gates, a short last group (the run's qubits not a
+        // multiple of max_q) is moved to the front: in a layer swept from the top qubit down, the
+        // low qubits then share a full group and the short group is on high qubits, where a
+        // group's accesses are contiguous across threads.
+        int limit = max_q;
+        if (!in_run && groupable(j)) {
+            int groups = 0, last_q = 0;
+            for (int64_t k = j; k >= 0 && groupable(k);) {
+                int nq = 0;
+                const int64_t kk = take_group(k, max_q, &nq);
+                if (k - kk < 2) break;
+                ++groups;
+                last_q = nq;
+                k = kk;
+            }
+            if (groups >= 2 && last_q < max_q) limit = last_q;
+        }
+        int64_t jj = take_group(j, limit, nullptr);
         if (j - jj >= 2) {
             steps.push_back({kSweepGroup, j, jj});
             j = jj;
+            in_run = true;
             continue;
         }
+        in_run = false;
         for (jj = j; jj >= 0 && n_params(jj) == 0; --jj) {}
         if (j - jj >= 2 && fusion != QI_FUSION_NONE) {
             int moves = 0;
@@ -736,20 +762,21 @@ extern "C" qi_status qi_adjoint_gradient(qi_state *s, const qi_gate *gates, int6
         if (plan.d_tc) cudaFree(plan.d_tc);
         if (!st.ok()) return bail(st);
     }
-    double ev[2] = {0, 0};
-    if (n_terms > 0) {
-        Status st = sumop_expectation(s, terms, n_terms, ev);
-        if (!st.ok()) return bail(st);
-    }
-    if (energy_out) *energy_out = ev[0];
-    // lambda = H psi
+    // lambda = H psi, and E = <psi|lambda> (one read pass of two states with FP64 sums, in place of
+    // one pass per X-mask group of H)
     qi_state *lam = nullptr;
     qi_status cs = qi_state_create(n, s->prec, &lam);
     if (cs != QI_OK) return bail(err(cs, -1, -1, "lambda state"));
     qi_state_set_stream(lam, s->stream);
     Status st = ok_status();
-    if (n_terms > 0) st = sumop_apply(lam, s, terms, n_terms);
-    else e = cudaMemsetAsync(lam->amps, 0, lam->bytes(), s->stream);
+    double ev[2] = {0, 0};
+    if (n_terms > 0) {
+        st = sumop_apply(lam, s, terms, n_terms);
+        if (st.ok()) st = state_inner(s, lam, ev);
+    } else {
+        e = cudaMemsetAsync(lam->amps, 0, lam->bytes(), s->stream);
+    }
+    if (energy_out) *energy_out = ev[0];
     // derivative slots (one per parameter of a gate; a gate group uses one per member)
     const int64_t nslots = 3 * n_gates + kMultiComps;
     double *d_gres = nullptr;

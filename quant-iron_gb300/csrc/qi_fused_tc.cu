@@ -266,7 +266,7 @@ struct TcCfg {
     static constexpr uint32_t LBO = 128;               // next core matrix along K
     static constexpr uint32_t SBO = (R / 4) * 128;     // next 8-row group along N
     // shared buffers: whole tiles, or (pair mode) a ring of units of 16 rows x 2 KB runs
-    static constexpr int NBUF = PAIR ? 10 : (K == 6 ? 2 : 6);
+    static constexpr int NBUF = PAIR ? (K == 6 ? 10 : 12) : (K == 6 ? 2 : 6);
     static constexpr uint32_t STAGE = 2 * R;           // TMEM columns of one A stage or one accumulator
     static constexpr uint32_t COL_A = 0, COL_D = 2 * STAGE;
     static constexpr uint32_t TMEM_COLS = 4 * STAGE;   // 512 for k = 6, 256 for k = 5
@@ -360,7 +360,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_fused_tc(float2 *a, const flo
                                                             const uint32_t *__restrict__ poly) {
     using C = TcCfg<K, PAIR>;
     constexpr int R = C::R, NB = C::NBUF;
-    static_assert(!PAIR || (K == 6 && C::UNIT_ROWS == C::CHUNK), "pair mode: K = 6, one ring unit per chunk");
+    static_assert(!PAIR || ((K == 5 || K == 6) && C::UNIT_ROWS == C::CHUNK), "pair mode: K = 5 or 6, one ring unit per chunk");
     static_assert(!(PAIR && ROT), "pair-mode tiles have qubit 0 as a column");
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     float *sB = reinterpret_cast<float *>(smem_raw);   // operand blocks (C::NBLK)
@@ -663,7 +663,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_fused_tc(float2 *a, const flo
                         }
                         mbar_arrive_expect_tx(raw_full + unit, C::BUF_BYTES);
                         unsigned char *dst = tiles + (size_t)unit * C::BUF_BYTES;
-                        const int row0 = 32 * (int)(u & 1u) + C::UNIT_ROWS * (int)(u >> 1);
+                        const int row0 = C::CONV_ROWS * (int)(u & 1u) + C::UNIT_ROWS * (int)(u >> 1);
                         for (int i = 0; i < C::UNIT_ROWS; ++i)
                             bulk_load(dst + (size_t)i * 2 * run_bytes, a + (base | grow[row0 + i]), 2 * run_bytes,
                                       raw_full + unit);
@@ -891,14 +891,14 @@ Status launch_fused_tc(qi_state *s, int k, const int32_t *targets, const void *d
     // differ in qubit L = 7, so each pair of runs is one 2 KB copy.  (Measured at 30 qubits: 3.28 ms
     // per launch against 4.4 ms for single tiles of 1 KB runs; a 4-unit ring with the N = 2R
     // imaginary half took 3.83 ms, so the ring depth matters more than the extra MMAs.)
-    const bool pair = k == 6 && g.nlow_t == 0 && g.nhigh == 6 && g.nfree >= 1 && g.L == 7 && g.L < n;
+    const bool pair = g.nlow_t == 0 && g.nhigh == k && g.nfree >= 1 && g.L == 7 && g.L < n;
     // qubits 0-3 all targets: lane-rotated row reads (k_fused_tc's ROT)
     bool rot = true;
     for (int q = 0; q < 4; ++q) rot = rot && std::find(targets, targets + k, q) != targets + k;
     if (poly && ((uintptr_t)poly & 15) != 0) return err(QI_ERR_UNKNOWN, -1, -1, "phase block must be 16-byte aligned");
 #define QI_TC(KK, PA, RO)                                                                    \
     (poly ? launch_tc_t<KK, PA, RO, true>(s, g, d_tc, poly) : launch_tc_t<KK, PA, RO, false>(s, g, d_tc, nullptr))
-    if (k == 5) return rot ? QI_TC(5, false, true) : QI_TC(5, false, false);
+    if (k == 5) return pair ? QI_TC(5, true, false) : rot ? QI_TC(5, false, true) : QI_TC(5, false, false);
     if (pair) return QI_TC(6, true, false);
     return rot ? QI_TC(6, false, true) : QI_TC(6, false, false);
 #undef QI_TC

@@ -62,13 +62,15 @@ def test_tensor_core_many_tiles_per_sm(qi, k):
     so every shared buffer, A stage and accumulator is reused and every
     barrier goes through both phases."""
     n = 23
-    # k = 6: [10..15] and [8, 10, ..., 18] take the tile-pair ring (all targets above qubit 7);
+    # k = 6: [10..15] and [8, 10, ..., 18] take the tile-pair ring (all targets above qubit 7),
+    # k = 5: [8, 11, 14, 18, 22] and [9..13];
     # [0..5], [0, 1, 2, 3, 9, 17] read row pairs in lane-rotated order (columns >= 128 B apart)
     # and store four rows at once; [0, 1, 4, 5, 12, 20] stores four rows without the rotation
     sets = {6: [[0, 1, 2, 3, 4, 5], [0, 6, 9, 17, 21, 22], [2, 3, 10, 15, 20, 22],
                 [10, 11, 12, 13, 14, 15], [7, 9, 11, 15, 19, 22], [0, 9, 13, 16, 20, 22],
                 [0, 1, 2, 3, 9, 17], [0, 1, 4, 5, 12, 20], [8, 10, 12, 14, 16, 18]],
-            5: [[0, 1, 2, 3, 4], [0, 7, 16, 21, 22], [1, 5, 12, 19, 22], [0, 1, 2, 3, 11]]}[k]
+            5: [[0, 1, 2, 3, 4], [0, 7, 16, 21, 22], [1, 5, 12, 19, 22], [0, 1, 2, 3, 11],
+                [8, 11, 14, 18, 22], [9, 10, 11, 12, 13]]}[k]
     init = rand_state(n, 5)
     for i, targets in enumerate(sets):
         U = haar(k, 100 + i)

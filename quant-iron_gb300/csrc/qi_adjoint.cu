@@ -334,7 +334,10 @@ __device__ __forceinline__ void multi_qubits(Amp *x, Amp *l, const MultiStageSme
 // column t of every buffer, so no block barrier is needed in the loop.  FP32 derivative
 // terms are summed in FP32 over batches of 16 items per thread and folded into FP64 per batch (an
 // FP64 add per item and stage would load the scarce FP64 pipe).
-template <typename T, int M, int S>
+// P0 (FP32, qubit 0 in the group): combos c and c | 1 are adjacent amplitudes, so each pair moves
+// as one 16-byte copy, read and stored as one 16-byte access (the group's items are 2^M
+// consecutive amplitudes; 8-byte copies would request every 32-byte sector four times).
+template <typename T, int M, int S, bool P0 = false>
 __global__ void __launch_bounds__(MultiShape<T>::kThreads, 1)
     k_adjoint_multi(typename MultiShape<T>::Amp *psi, typename MultiShape<T>::Amp *lam,
                     const __grid_constant__ MultiParams p, double *partials) {
@@ -353,16 +356,23 @@ __global__ void __launch_bounds__(MultiShape<T>::kThreads, 1)
     auto slot = [&](int stage, int which, int c) -> Amp * {
         return buf + (((size_t)stage * 2 + which) * D + c) * TH + t;
     };
+    // P0: pair cp (combos 2cp, 2cp + 1) of thread t, 16 bytes
+    auto slot2 = [&](int stage, int which, int cp) -> Amp * {
+        return buf + ((((size_t)stage * 2 + which) * (D / 2) + cp) * TH + t) * 2;
+    };
     auto issue = [&](uint64_t w, int stage) {
         if (w < p.nwork) {
             const uint64_t base = insert_zeros(w, p.pos, M);
 #pragma unroll
-            for (int c = 0; c < D; ++c) {
+            for (int c = 0; c < D; c += (P0 ? 2 : 1)) {
                 uint64_t o = base;
 #pragma unroll
                 for (int i = 0; i < M; ++i)
                     if ((c >> i) & 1) o |= bitm[i];
-                if constexpr (sizeof(Amp) == 8) {
+                if constexpr (P0) {
+                    cp_async_16(slot2(stage, 0, c >> 1), psi + o);
+                    cp_async_16(slot2(stage, 1, c >> 1), lam + o);
+                } else if constexpr (sizeof(Amp) == 8) {
                     cp_async_8(slot(stage, 0, c), psi + o);
                     cp_async_8(slot(stage, 1, c), lam + o);
                 } else {
@@ -390,23 +400,40 @@ __global__ void __launch_bounds__(MultiShape<T>::kThreads, 1)
         for (uint64_t w = wb; w < wend; w += stride) {
             cp_async_wait<PIPE - 2>();   // this item's group has landed
             Amp x[D], l[D];
+            if constexpr (P0) {
 #pragma unroll
-            for (int c = 0; c < D; ++c) {
-                x[c] = *slot(stage, 0, c);
-                l[c] = *slot(stage, 1, c);
+                for (int c = 0; c < D; c += 2) {
+                    const ulonglong2 u = *reinterpret_cast<const ulonglong2 *>(slot2(stage, 0, c >> 1));
+                    const ulonglong2 v = *reinterpret_cast<const ulonglong2 *>(slot2(stage, 1, c >> 1));
+                    x[c] = u.x;
+                    x[c + 1] = u.y;
+                    l[c] = v.x;
+                    l[c + 1] = v.y;
+                }
+            } else {
+#pragma unroll
+                for (int c = 0; c < D; ++c) {
+                    x[c] = *slot(stage, 0, c);
+                    l[c] = *slot(stage, 1, c);
+                }
             }
             // refill the buffer read one iteration ago (only this thread uses its column)
             issue(w + (PIPE - 1) * stride, stage == 0 ? PIPE - 1 : stage - 1);
             multi_qubits<T, M, S, 0>(x, l, sm, accb);
             const uint64_t base = insert_zeros(w, p.pos, M);
 #pragma unroll
-            for (int c = 0; c < D; ++c) {
+            for (int c = 0; c < D; c += (P0 ? 2 : 1)) {
                 uint64_t o = base;
 #pragma unroll
                 for (int i = 0; i < M; ++i)
                     if ((c >> i) & 1) o |= bitm[i];
-                psi[o] = x[c];
-                lam[o] = l[c];
+                if constexpr (P0) {
+                    *reinterpret_cast<ulonglong2 *>(psi + o) = make_ulonglong2(x[c], x[c + 1]);
+                    *reinterpret_cast<ulonglong2 *>(lam + o) = make_ulonglong2(l[c], l[c + 1]);
+                } else {
+                    psi[o] = x[c];
+                    lam[o] = l[c];
+                }
             }
             stage = stage == PIPE - 1 ? 0 : stage + 1;
         }
@@ -423,12 +450,12 @@ __global__ void __launch_bounds__(MultiShape<T>::kThreads, 1)
 
 // One block per SM slot the shared-memory pipeline leaves (grid-stride over the work items);
 // *nb_out = blocks launched (= partial-sum rows).
-template <typename T, int M, int S>
+template <typename T, int M, int S, bool P0 = false>
 static Status launch_adjoint_multi(qi_state *s, qi_state *lam, const MultiParams &mp, unsigned *nb_out) {
     using Amp = typename MultiShape<T>::Amp;
     constexpr int TH = MultiShape<T>::kThreads;
     const size_t smem = (size_t)MultiShape<T>::kPipe * 2 * (1 << M) * TH * sizeof(Amp);
-    auto kern = k_adjoint_multi<T, M, S>;
+    auto kern = k_adjoint_multi<T, M, S, P0>;
     static std::atomic<int> per_sm_of[64];   // per instantiation and device: blocks per SM, 0 = not set up
     static std::atomic<int> sms_of[64];
     int dev = 0;
@@ -609,49 +636,31 @@ static std::vector<SweepStep> plan_reverse_sweep(const std::vector<GateMatrix> &
         return !m.pauli && m.nt == 1 && m.controls.empty() && n_params(jj) <= 1;
     };
     const int max_q = f32 ? kMultiQubits : kMultiQubits - 1;   // FP64 x 16 amplitudes spills
-    // One group from gate j down, at most `limit` qubits; returns the gate below it.
-    auto take_group = [&](int64_t j, int limit, int *nq) {
+    // One group from gate j down, at most max_q qubits; returns the gate below it.
+    auto take_group = [&](int64_t j) {
         int qcount[64] = {0};
         uint64_t qmask = 0;
         int64_t jj = j;
         for (; jj >= 0 && groupable(jj); --jj) {
             const int q = mats[(size_t)jj].t[0];
-            if (!((qmask >> q) & 1ull) && __builtin_popcountll(qmask) == limit) break;
+            if (!((qmask >> q) & 1ull) && __builtin_popcountll(qmask) == max_q) break;
             if (qcount[q] == kMultiStages) break;
             qmask |= 1ull << q;
             ++qcount[q];
         }
-        if (nq) *nq = __builtin_popcountll(qmask);
         return jj;
     };
     std::vector<SweepStep> steps;
-    bool in_run = false;   // the previous pass was a group ending where this one starts
     for (int64_t j = n_gates - 1; j >= 0;) {
-        // At the start of a run of groupable gates, a short last group (the run's qubits not a
-        // multiple of max_q) is moved to the front: in a layer swept from the top qubit down, the
-        // low qubits then share a full group and the short group is on high qubits, where a
-        // group's accesses are contiguous across threads.
-        int limit = max_q;
-        if (!in_run && groupable(j)) {
-            int groups = 0, last_q = 0;
-            for (int64_t k = j; k >= 0 && groupable(k);) {
-                int nq = 0;
-                const int64_t kk = take_group(k, max_q, &nq);
-                if (k - kk < 2) break;
-                ++groups;
-                last_q = nq;
-                k = kk;
-            }
-            if (groups >= 2 && last_q < max_q) limit = last_q;
-        }
-        int64_t jj = take_group(j, limit, nullptr);
+        // (Putting a run's short group first, on the high qubits, so that the low qubits share a
+        // full group, measured slower: a group on qubits 0-3 took 1.15 ms at 26 qubits against
+        // 0.55 ms for qubits 0-1 and 0.42 ms for 2-5.)
+        int64_t jj = take_group(j);
         if (j - jj >= 2) {
             steps.push_back({kSweepGroup, j, jj});
             j = jj;
-            in_run = true;
             continue;
         }
-        in_run = false;
         for (jj = j; jj >= 0 && n_params(jj) == 0; --jj) {}
         if (j - jj >= 2 && fusion != QI_FUSION_NONE) {
             int moves = 0;
@@ -878,7 +887,9 @@ extern "C" qi_status qi_adjoint_gradient(qi_state *s, const qi_gate *gates, int6
             if (!st.ok()) break;
             mp.nwork = 1ull << (n - M);
             unsigned nb = 1;
-#define QI_AM(T, MM, SS) st = launch_adjoint_multi<T, MM, SS>(s, lam, mp, &nb)
+#define QI_AM(T, MM, SS)                                                                         \
+    st = (sizeof(T) == 4 && mp.pos[0] == 0) ? launch_adjoint_multi<T, MM, SS, sizeof(T) == 4>(s, lam, mp, &nb) \
+                                            : launch_adjoint_multi<T, MM, SS>(s, lam, mp, &nb)
 #define QI_AM_S(T, MM) { if (S == 1) QI_AM(T, MM, 1); else QI_AM(T, MM, 2); }
             if (f32) {
                 if (M == 1) QI_AM_S(float, 1) else if (M == 2) QI_AM_S(float, 2)

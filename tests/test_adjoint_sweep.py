@@ -36,29 +36,22 @@ def check_sweep(qi, gates, steps, f32, fusion_on):
     n = len(gates)
     expect_hi = n - 1
     max_q = 4 if f32 else 3
-    prev_kind = None
     for kind, hi, lo in steps:
         assert hi == expect_hi and lo < hi
         run = [gates[k] for k in range(hi, lo, -1)]   # sweep order
         expect_hi = lo
         if kind == qi.SWEEP_GATE:
             assert hi - lo == 1
-            prev_kind = kind
             continue
         assert hi - lo >= 2
         if kind == qi.SWEEP_GROUP:
             assert all(groupable(qi, g) for g in run)
             qs = [int(g["targets"][0]) for g in run]
             assert len(set(qs)) <= max_q and max(qs.count(q) for q in qs) <= 2
-            first_of_run = prev_kind != qi.SWEEP_GROUP
-            if lo >= 0 and groupable(qi, gates[lo]) and not first_of_run:
-                # maximal: the next gate would break a limit (a run's first group may be cut
-                # short so that its last group is full)
+            if lo >= 0 and groupable(qi, gates[lo]):   # maximal: the next gate would break a limit
                 q = int(gates[lo]["targets"][0])
                 assert (q not in qs and len(set(qs)) == max_q) or qs.count(q) == 2
-            prev_kind = kind
             continue
-        prev_kind = kind
         assert fusion_on
         assert all(gate_info(qi, g)[1] == 0 for g in run)
         moves = [g for g in run if gate_info(qi, g)[0] != "IDENTITY"]
@@ -121,11 +114,11 @@ def test_random_sweeps_obey_the_rules(qi, seed, prec):
 
 def test_hea_26_sweep_structure(qi):
     """12 layers of RY.RZ on 26 qubits + a CNOT ladder: per layer one permutation for the
-    ladder and 7 group passes (1 x 2 qubits, on qubits 25 and 24, then 6 x 4 qubits x 2 gates down
-    to qubit 0) in FP32, 9 in FP64 (3 qubits per group); no per-gate passes."""
+    ladder and 7 group passes (6 x 4 qubits x 2 gates + 1 x 2 qubits) in FP32, 9 in FP64
+    (3 qubits per group); no per-gate passes."""
     n, layers = 26, 12
     gates, theta = workloads.hea_ansatz(n, layers, seed=1)
-    for prec, per_layer in ((1, [4] + [8] * 6), (0, [4] + [6] * 8)):   # gates per group pass
+    for prec, per_layer in ((1, [8] * 6 + [4]), (0, [6] * 8 + [4])):   # gates per group pass
         steps = qi.adjoint_sweep_plan(n, prec, gates, theta)
         check_sweep(qi, gates, steps, prec == 1, True)
         assert len(steps) == layers * (1 + len(per_layer))

@@ -457,8 +457,8 @@ def costmodel_eval(qi, workloads, torch, np, n_train=28, count=4000, qubits=rang
     """The learned-fusion configuration: the cost model trained on `count` engine-timed blocks
     at n_train qubits, then seeded random circuits of the benchmark family (one per qubit count
     in `qubits`, depth 20-60) planned three ways — greedy fixed-k, the learned choice, and (up to
-    `exhaustive_upto` qubits) exhaustive timing of every preset partition — with measured wall
-    time as the judge, and the learned plan's infidelity against the FP64 per-gate path up to
+    `exhaustive_upto` qubits) exhaustive timing of every preset partition — compared by measured
+    wall time, and the learned plan's infidelity against the FP64 per-gate path up to
     33 qubits (FP64 at 34 qubits would need 256 GiB)."""
     from quant_iron_gb300 import costmodel
     t0 = time.perf_counter()
@@ -722,7 +722,7 @@ def main():
     if dom == "k_fused_tc" and os.path.exists(prof):
         pj = json.load(open(prof))
         traffic = pj["traffic_per_amp_bytes"] * (1 << n)
-        traffic_src = "profiles/k_fused_tc_fused26.md (26-qubit capture x 2^%d)" % (n - 26)
+        traffic_src = "ncu dram__bytes_read.sum + dram__bytes_write.sum of a 26-qubit k_fused_tc launch, x 2^%d" % (n - 26)
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": traffic, "traffic_source": traffic_src, "kernel": dom, "peak_source": peak_kind,
                 "algorithmic_bytes_per_launch": pass_bytes, "avg_launch_ms": avg_ms,

@@ -782,6 +782,9 @@ extern "C" qi_status qi_adjoint_gradient(qi_state *s, const qi_gate *gates, int6
     if (n_terms > 0) {
         st = sumop_apply(lam, s, terms, n_terms);
         if (st.ok()) st = state_inner(s, lam, ev);
+        int flag = 0;
+        if (st.ok()) st = state_read_flag(lam, &flag);
+        if (st.ok() && flag == 2) st = err(QI_ERR_TIMEOUT, -1, -1, "SumOp::apply: a device wait timed out");
     } else {
         e = cudaMemsetAsync(lam->amps, 0, lam->bytes(), s->stream);
     }

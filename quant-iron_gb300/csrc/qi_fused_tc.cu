@@ -44,6 +44,7 @@
 // accumulator d at 4R + d*2R (D_re [0,R), D_im [R,2R)): 8R columns in all.
 #include "qi_internal.hpp"
 #include "qi_device.cuh"
+#include "qi_async.cuh"
 #include "qi_tile.cuh"
 
 #include <algorithm>
@@ -55,48 +56,8 @@ namespace qi {
 constexpr int kConvWarps = 8, kEpiWarps = 4;
 constexpr int kProducerWarp = kConvWarps + kEpiWarps, kMmaWarp = kProducerWarp + 1;
 constexpr int kTcThreads = (kMmaWarp + 1) * 32;   // 448
-// Every mbarrier wait gives up after kWaitNs of wall time (%globaltimer), or after
-// kWaitLimit polls should the timer not advance; a single try_wait may suspend
-// the thread for a hardware-defined time, so the clock is the real bound.
-constexpr uint64_t kWaitNs = 2000000000ull;   // 2 s
-constexpr uint32_t kWaitLimit = 1u << 26;
 
 // ---------------------------------------------------------- PTX wrappers --
-__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
-    uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}\n"
-        : "=r"(ok)
-        : "r"(smem_u32(bar)), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-
-__device__ __forceinline__ uint64_t global_ns() {
-    uint64_t t;
-    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-    return t;
-}
-
-// Bounded wait: false if the phase did not complete within kWaitNs.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity) {
-    if (mbar_try_wait(bar, parity)) return true;
-    const uint64_t t0 = global_ns();
-    for (uint32_t i = 0; i < kWaitLimit; ++i) {
-        if (mbar_try_wait(bar, parity)) return true;
-        if ((i & 31u) == 31u && global_ns() - t0 > kWaitNs) return false;
-    }
-    return false;
-}
-
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory"); }
 
@@ -212,38 +173,6 @@ __device__ __forceinline__ void tmem_ld<32>(uint32_t taddr, uint32_t (&v)[32]) {
 __device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;\n" ::: "memory"); }
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory"); }
 
-__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
-    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(smem_u32(bar)) : "memory");
-}
-__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, uint32_t bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(bytes)
-                 : "memory");
-}
-// Contiguous global -> shared copy on the bulk-copy engine; completes `bytes`
-// of the barrier's transaction count.  Both addresses 16-byte aligned, bytes % 16 == 0.
-__device__ __forceinline__ void bulk_load(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
-    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
-                     smem_u32(dst)),
-                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
-                 : "memory");
-}
-
-// Bounded wait that also gives up when another role raised the abort flag;
-// a timeout raises it and records status 2 in the state's error flag.
-__device__ __forceinline__ bool wait_or_abort(uint64_t *bar, uint32_t parity, volatile int *abort_flag, int *err_flag) {
-    if (mbar_try_wait(bar, parity)) return true;
-    const uint64_t t0 = global_ns();
-    for (uint32_t i = 0; i < kWaitLimit; ++i) {
-        if (mbar_try_wait(bar, parity)) return true;
-        if ((i & 31u) == 31u) {
-            if (*abort_flag) return false;
-            if (global_ns() - t0 > kWaitNs) break;
-        }
-    }
-    *abort_flag = 1;
-    atomicExch(err_flag, 2);   // 2 = a bounded device wait ran out (1 is ZeroNorm)
-    return false;
-}
 // Warp-uniform form: every lane waits, the warp proceeds only if all saw the phase.
 __device__ __forceinline__ bool warp_wait_or_abort(uint64_t *bar, uint32_t parity, volatile int *abort_flag,
                                                    int *err_flag) {

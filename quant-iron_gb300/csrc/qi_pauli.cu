@@ -12,6 +12,7 @@
 // the pair (i, i ^ xmask) and writes both outputs.
 #include "qi_internal.hpp"
 #include "qi_device.cuh"
+#include "qi_async.cuh"
 
 #include <algorithm>
 #include <cmath>
@@ -902,6 +903,145 @@ __global__ void __launch_bounds__(256) k_sumop_apply_f32(float2 *o, const float2
     }
 }
 
+// Streamed FP32 SumOp::apply for states of 2^kApplyTileBits amplitudes and more.  The output is
+// taken in tiles of 2^kApplyTileBits consecutive amplitudes; a group with X mask x reads, for
+// output tile T, the input tile T ^ (x >> kApplyTileBits) at local offsets l ^ (x & tile mask).
+// The groups are ordered by that tile offset (one step per distinct offset, offset 0 first), so
+// each step is one contiguous 32 KB bulk copy into a ring of shared-memory buffers and every
+// gather becomes a shared-memory read.  Roles: 16 compute warps, and one copy warp whose lane 0
+// issues the copies as soon as the compute warps release a buffer (full / empty mbarriers per
+// buffer; no block-wide barrier in the loop, every wait bounded).
+// Factors: compute thread t owns the amplitudes l_j = t + 512 j (j = 0..7) of a tile, whose
+// indices differ only in bits 9-11.  A term with Z mask z contributes c (-1)^popc(i_j & z) =
+// c (-1)^popc(b & z) (-1)^popc(j & m), b = tile bits | t, m = bits 9-11 of z; so the thread sums
+// each group's terms once per tile into A[m] (terms are sorted by m on the host) and an 8-point
+// Walsh-Hadamard transform of A gives the factors of all eight amplitudes (one term evaluation per
+// eight amplitudes instead of one per amplitude).
+constexpr int kApplyTileBits = 12, kApplyTileAmps = 1 << kApplyTileBits;
+constexpr int kApplyTileThreads = 512, kApplyTileBufs = 6;
+constexpr int kApplyComputeWarps = kApplyTileThreads / 32;
+constexpr int kApplyBlockThreads = kApplyTileThreads + 32;             // + the copy warp
+constexpr int kApplyTilePer = kApplyTileAmps / kApplyTileThreads;   // 8 amplitudes per thread
+static_assert(kApplyTileThreads == 512 && kApplyTilePer == 8, "bits 9-11 of a tile index select the amplitude");
+struct ApplyStep {
+    uint64_t tile_xor;        // input tile = output tile ^ tile_xor
+    int32_t g_first, g_count;  // its groups
+};
+struct TileGroup {
+    uint32_t xl;       // X mask bits below the tile size
+    int32_t m[9];      // terms with bits 9-11 of the Z mask = m: [m[m], m[m + 1])
+};
+template <typename IDX> struct TileTerm {
+    IDX z;
+    float re, im;
+};
+
+template <typename IDX>
+__global__ void __launch_bounds__(kApplyBlockThreads, 1)
+    k_sumop_apply_tiles_f32(float2 *o, const float2 *in, uint64_t ntiles, const ApplyStep *steps, int nsteps,
+                            const TileGroup *groups, int ngroups, const TileTerm<IDX> *terms, int nterms,
+                            int *err_flag) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float2 *buf = reinterpret_cast<float2 *>(smem_raw);                          // [kApplyTileBufs][tile]
+    ApplyStep *sstep = reinterpret_cast<ApplyStep *>(buf + (size_t)kApplyTileBufs * kApplyTileAmps);
+    TileTerm<IDX> *sterm = reinterpret_cast<TileTerm<IDX> *>(sstep + nsteps);
+    TileGroup *sgrp = reinterpret_cast<TileGroup *>(sterm + nterms);
+    __shared__ __align__(8) uint64_t full[kApplyTileBufs], empty[kApplyTileBufs];
+    __shared__ int abort_flag;
+    volatile int *abort_v = &abort_flag;
+    const int tid = threadIdx.x;
+    for (int k = tid; k < nsteps; k += blockDim.x) sstep[k] = steps[k];
+    for (int k = tid; k < nterms; k += blockDim.x) sterm[k] = terms[k];
+    for (int k = tid; k < ngroups; k += blockDim.x) sgrp[k] = groups[k];
+    if (tid == 0) {
+        for (int b = 0; b < kApplyTileBufs; ++b) {
+            mbar_init(full + b, 1);
+            mbar_init(empty + b, kApplyComputeWarps);
+        }
+        abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    __syncthreads();
+    constexpr uint32_t kBytes = kApplyTileAmps * sizeof(float2);
+    const uint64_t mine = blockIdx.x < ntiles ? (ntiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+    const uint64_t total = mine * (uint64_t)nsteps;   // (tile, step) pairs of this block, in order
+    if (tid >= kApplyTileThreads) {
+        // ------------------------------------------------ copy warp (lane 0)
+        if (tid == kApplyTileThreads) {
+            uint64_t issued = 0;
+            for (; issued < total; ++issued) {
+                const int b = (int)(issued % kApplyTileBufs);
+                if (issued >= (uint64_t)kApplyTileBufs &&
+                    !wait_or_abort(empty + b, (uint32_t)(issued / kApplyTileBufs - 1) & 1u, abort_v, err_flag))
+                    break;
+                const uint64_t it = issued / (uint64_t)nsteps;
+                const uint64_t src = (blockIdx.x + it * gridDim.x) ^ sstep[issued - it * nsteps].tile_xor;
+                mbar_arrive_expect_tx(full + b, kBytes);
+                bulk_load(buf + (size_t)b * kApplyTileAmps, in + (src << kApplyTileBits), kBytes, full + b);
+            }
+            // the last copies land before the block exits (after an abort, unread ones too)
+            for (uint64_t k = issued > (uint64_t)kApplyTileBufs ? issued - kApplyTileBufs : 0; k < issued; ++k)
+                if (!mbar_wait_bounded(full + (k % kApplyTileBufs), (uint32_t)(k / kApplyTileBufs) & 1u))
+                    atomicExch(err_flag, 2);
+        }
+        return;
+    }
+    // ---------------------------------------------------- compute warps
+    const int lane = tid & 31;
+    float2 acc[kApplyTilePer];
+    for (uint64_t q = 0; q < total; ++q) {
+        const uint64_t it = q / (uint64_t)nsteps;
+        const int st = (int)(q - it * nsteps);
+        const uint64_t tile = blockIdx.x + it * gridDim.x;
+        if (st == 0) {
+#pragma unroll
+            for (int j = 0; j < kApplyTilePer; ++j) acc[j] = make_float2(0.0f, 0.0f);
+        }
+        const int b = (int)(q % kApplyTileBufs);
+        const bool ok = wait_or_abort(full + b, (uint32_t)(q / kApplyTileBufs) & 1u, abort_v, err_flag);
+        if (!__all_sync(0xffffffffu, ok)) break;
+        const float2 *P = buf + (size_t)b * kApplyTileAmps;
+        const ApplyStep stp = sstep[st];
+        const IDX base = (IDX)((tile << kApplyTileBits) | (uint64_t)tid);   // bits 9-11 clear
+        for (int g = stp.g_first; g < stp.g_first + stp.g_count; ++g) {
+            const TileGroup &G = sgrp[g];
+            float2 A[8];
+#pragma unroll
+            for (int m = 0; m < 8; ++m) {
+                float re = 0.0f, im = 0.0f;
+                for (int k = G.m[m]; k < G.m[m + 1]; ++k) {
+                    const TileTerm<IDX> t = sterm[k];
+                    const uint32_t par = (uint32_t)(sizeof(IDX) == 4 ? __popc((uint32_t)(base & t.z))
+                                                                    : __popcll((uint64_t)(base & t.z)));
+                    const uint32_t sb = par << 31;   // the parity's sign, as an FP32 sign bit
+                    re += __uint_as_float(__float_as_uint(t.re) ^ sb);
+                    im += __uint_as_float(__float_as_uint(t.im) ^ sb);
+                }
+                A[m] = make_float2(re, im);
+            }
+#pragma unroll
+            for (int h = 1; h < 8; h <<= 1)   // f[j] = sum_m A[m] (-1)^popc(j & m)
+#pragma unroll
+                for (int m = 0; m < 8; ++m)
+                    if (!(m & h)) {
+                        const float2 u = A[m], v = A[m | h];
+                        A[m] = make_float2(u.x + v.x, u.y + v.y);
+                        A[m | h] = make_float2(u.x - v.x, u.y - v.y);
+                    }
+#pragma unroll
+            for (int j = 0; j < kApplyTilePer; ++j)
+                acc[j] = Cx<float>::fma(A[j], P[(uint32_t)(tid + j * kApplyTileThreads) ^ G.xl], acc[j]);
+        }
+        __syncwarp();
+        if (lane == 0) mbar_arrive(empty + b);   // this warp is done with buffer b
+        if (st == nsteps - 1) {
+#pragma unroll
+            for (int j = 0; j < kApplyTilePer; ++j)
+                o[(tile << kApplyTileBits) | (uint64_t)(tid + j * kApplyTileThreads)] = acc[j];
+        }
+    }
+}
+
 // Host side of k_sumop_apply_f32: term records, the byte tables of the largest group (moved
 // to index 0) and the shared-memory size.
 template <typename IDX>
@@ -961,13 +1101,86 @@ static void build_apply_plan(int n, const std::vector<GroupHdr> &hdrs, const std
     }
 }
 
+// The streamed form: groups ordered by input-tile offset (offset 0 first), one step per offset,
+// each group's terms sorted by bits 9-11 of their Z masks.  *done = false (nothing launched) when
+// the state is smaller than a tile or the records do not fit beside the ring.
+template <typename IDX>
+static Status launch_sumop_apply_tiles_f32(qi_state *o, qi_state *in, const std::vector<GroupHdr> &hdrs,
+                                           const std::vector<GroupTerm> &gts, bool *done) {
+    *done = false;
+    if (o->n < kApplyTileBits) return ok_status();
+    std::map<uint64_t, std::vector<size_t>> by_off;
+    for (size_t g = 0; g < hdrs.size(); ++g) by_off[hdrs[g].xmask >> kApplyTileBits].push_back(g);
+    std::vector<ApplyStep> steps;
+    std::vector<TileGroup> groups;
+    std::vector<TileTerm<IDX>> terms;
+    for (auto &kv : by_off) {
+        ApplyStep stp;
+        stp.tile_xor = kv.first;
+        stp.g_first = (int32_t)groups.size();
+        stp.g_count = (int32_t)kv.second.size();
+        for (size_t g : kv.second) {
+            const GroupHdr &h = hdrs[g];
+            TileGroup tg;
+            tg.xl = (uint32_t)(h.xmask & (uint64_t)(kApplyTileAmps - 1));
+            for (int m = 0; m < 8; ++m) {
+                tg.m[m] = (int32_t)terms.size();
+                for (int k = 0; k < h.count; ++k) {
+                    const GroupTerm &t = gts[(size_t)(h.first + k)];
+                    if ((int)((t.zmask >> 9) & 7) == m)
+                        terms.push_back(TileTerm<IDX>{(IDX)t.zmask, (float)t.re, (float)t.im});
+                }
+            }
+            tg.m[8] = (int32_t)terms.size();
+            groups.push_back(tg);
+        }
+        steps.push_back(stp);
+    }
+    const size_t ring = (size_t)kApplyTileBufs * kApplyTileAmps * sizeof(float2);
+    const size_t meta = steps.size() * sizeof(ApplyStep) + terms.size() * sizeof(TileTerm<IDX>) +
+                        groups.size() * sizeof(TileGroup);
+    const size_t sm = ring + meta;
+    if (sm > 220 * 1024) return ok_status();
+    int dev = 0, sms = 0;
+    QI_CUDA(cudaGetDevice(&dev));
+    QI_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    // one device block for the records, each array starting on a 16-byte boundary
+    auto up16 = [](size_t v) { return (v + 15) & ~(size_t)15; };
+    const size_t off_term = up16(steps.size() * sizeof(ApplyStep));
+    const size_t off_grp = off_term + up16(std::max<size_t>(1, terms.size()) * sizeof(TileTerm<IDX>));
+    const size_t bytes = off_grp + up16(groups.size() * sizeof(TileGroup));
+    unsigned char *d = nullptr;
+    QI_CUDA(cudaMallocAsync((void **)&d, bytes, o->stream));
+    ApplyStep *d_steps = reinterpret_cast<ApplyStep *>(d);
+    TileTerm<IDX> *d_term = reinterpret_cast<TileTerm<IDX> *>(d + off_term);
+    TileGroup *d_grp = reinterpret_cast<TileGroup *>(d + off_grp);
+    QI_CUDA(cudaMemcpyAsync(d_steps, steps.data(), steps.size() * sizeof(ApplyStep), cudaMemcpyHostToDevice, o->stream));
+    if (!terms.empty())
+        QI_CUDA(cudaMemcpyAsync(d_term, terms.data(), terms.size() * sizeof(TileTerm<IDX>), cudaMemcpyHostToDevice,
+                                o->stream));
+    QI_CUDA(cudaMemcpyAsync(d_grp, groups.data(), groups.size() * sizeof(TileGroup), cudaMemcpyHostToDevice, o->stream));
+    auto kern = k_sumop_apply_tiles_f32<IDX>;
+    QI_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    const uint64_t ntiles = o->dim() >> kApplyTileBits;
+    const unsigned grid = (unsigned)std::min<uint64_t>(ntiles, (uint64_t)std::max(sms, 1));
+    kern<<<grid, kApplyBlockThreads, sm, o->stream>>>((float2 *)o->amps, (const float2 *)in->amps, ntiles, d_steps,
+                                                     (int)steps.size(), d_grp, (int)groups.size(), d_term,
+                                                     (int)terms.size(), o->d_flag);
+    count_launch();
+    Status st = check_launch("k_sumop_apply_tiles_f32");
+    QI_CUDA(cudaFreeAsync(d, o->stream));
+    *done = st.ok();
+    return st;
+}
+
 template <typename IDX>
 static Status launch_sumop_apply_f32(qi_state *o, qi_state *in, const std::vector<GroupHdr> &hdrs,
                                      const std::vector<GroupTerm> &gts, bool *done) {
+    Status tst = launch_sumop_apply_tiles_f32<IDX>(o, in, hdrs, gts, done);
+    if (!tst.ok() || *done) return tst;
     ApplyPlan<IDX> ap;
     build_apply_plan<IDX>(o->n, hdrs, gts, ap);
     const size_t sm = ap.smem();
-    *done = false;
     if (sm > 200 * 1024) return ok_status();   // the caller takes the generic kernel
     ApplyHdr<IDX> *d_hdr = nullptr;
     ApplyTerm<IDX> *d_term = nullptr;
@@ -1298,7 +1511,12 @@ qi_status qi_sumop_apply(qi_state *out, qi_state *in, const qi_pauli_term *terms
         if (!st.ok()) return publish(st);
         return publish(state_scale_async(out, 0.0, 0.0));
     }
-    return publish(sumop_apply(out, in, terms, n_terms));
+    Status st = sumop_apply(out, in, terms, n_terms);
+    if (!st.ok()) return publish(st);
+    int flag = 0;
+    st = state_read_flag(out, &flag);
+    if (st.ok() && flag == 2) st = err(QI_ERR_TIMEOUT, -1, -1, "SumOp::apply: a device wait timed out");
+    return publish(st);
 }
 
 qi_status qi_sumop_expectation(qi_state *s, const qi_pauli_term *terms, int64_t n_terms, double out[2]) {

@@ -91,6 +91,24 @@ def test_sumop_apply_f32_tabled_group(qi, orc, case):
     assert np.max(np.abs(got - want)) < 2e-6 * scale
 
 
+@pytest.mark.parametrize("n", [11, 12, 17, 22])
+def test_sumop_apply_f32_streamed_tiles(qi, orc, n):
+    """FP32 SumOp::apply from states of 2^12 amplitudes up streams input tiles through shared
+    memory, one step per distinct X-mask offset above the tile: random terms of weight up to 4
+    on every qubit give dozens of steps (the copy ring wraps many times), n = 22 gives several
+    tiles per block; n = 11 takes the per-element gather kernel."""
+    init = rand_state(n, 40 + n)
+    terms = rand_terms(n, 60, 70 + n, max_weight=4)
+    want = orc.sumop_apply(init, n, terms)
+    with qi.DeviceState(n, 1) as st, qi.DeviceState(n, 1) as out:
+        st.upload(init)
+        qi.sumop_apply(out, st, terms)
+        got = out.download()
+        assert np.max(np.abs(st.download() - init)) < 1e-6   # the input is left as it was
+    scale = float(np.sum(np.abs(terms["re"]) + np.abs(terms["im"])))
+    assert np.max(np.abs(got - want)) < 2e-6 * scale
+
+
 def test_heisenberg_expectation_20q(qi, orc):
     n = 20
     init = rand_state(n, 1)

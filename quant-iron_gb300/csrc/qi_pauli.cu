@@ -930,8 +930,9 @@ struct ApplyStep {
 struct TileGroup {
     uint32_t xl;       // X mask bits below the tile size
     int32_t m[9];      // terms with bits 9-11 of the Z mask = m: [m[m], m[m + 1])
+    int32_t flat;      // 1: every term has m = 0 (one factor for all eight amplitudes, no transform)
 };
-template <typename IDX> struct TileTerm {
+template <typename IDX> struct alignas(16) TileTerm {   // one 16-byte shared-memory load
     IDX z;
     float re, im;
 };
@@ -968,16 +969,22 @@ __global__ void __launch_bounds__(kApplyBlockThreads, 1)
     if (tid >= kApplyTileThreads) {
         // ------------------------------------------------ copy warp (lane 0)
         if (tid == kApplyTileThreads) {
-            uint64_t issued = 0;
+            uint64_t issued = 0, tile = blockIdx.x;
+            int st = 0, b = 0;
+            uint32_t phase = 0;   // of empty[b]: the compute warps' release of the buffer's previous fill
             for (; issued < total; ++issued) {
-                const int b = (int)(issued % kApplyTileBufs);
-                if (issued >= (uint64_t)kApplyTileBufs &&
-                    !wait_or_abort(empty + b, (uint32_t)(issued / kApplyTileBufs - 1) & 1u, abort_v, err_flag))
-                    break;
-                const uint64_t it = issued / (uint64_t)nsteps;
-                const uint64_t src = (blockIdx.x + it * gridDim.x) ^ sstep[issued - it * nsteps].tile_xor;
+                if (issued >= (uint64_t)kApplyTileBufs && !wait_or_abort(empty + b, phase, abort_v, err_flag)) break;
+                const uint64_t src = tile ^ sstep[st].tile_xor;
                 mbar_arrive_expect_tx(full + b, kBytes);
                 bulk_load(buf + (size_t)b * kApplyTileAmps, in + (src << kApplyTileBits), kBytes, full + b);
+                if (++b == kApplyTileBufs) {
+                    b = 0;
+                    if (issued >= (uint64_t)kApplyTileBufs) phase ^= 1u;
+                }
+                if (++st == nsteps) {
+                    st = 0;
+                    tile += gridDim.x;
+                }
             }
             // the last copies land before the block exits (after an abort, unread ones too)
             for (uint64_t k = issued > (uint64_t)kApplyTileBufs ? issued - kApplyTileBufs : 0; k < issued; ++k)
@@ -989,22 +996,38 @@ __global__ void __launch_bounds__(kApplyBlockThreads, 1)
     // ---------------------------------------------------- compute warps
     const int lane = tid & 31;
     float2 acc[kApplyTilePer];
+    // (tile, step, buffer, phase) advance by counting: no divisions in the loop
+    uint64_t tile = blockIdx.x;
+    int st = 0, b = 0;
+    uint32_t phase = 0;
     for (uint64_t q = 0; q < total; ++q) {
-        const uint64_t it = q / (uint64_t)nsteps;
-        const int st = (int)(q - it * nsteps);
-        const uint64_t tile = blockIdx.x + it * gridDim.x;
         if (st == 0) {
 #pragma unroll
             for (int j = 0; j < kApplyTilePer; ++j) acc[j] = make_float2(0.0f, 0.0f);
         }
-        const int b = (int)(q % kApplyTileBufs);
-        const bool ok = wait_or_abort(full + b, (uint32_t)(q / kApplyTileBufs) & 1u, abort_v, err_flag);
+        const bool ok = wait_or_abort(full + b, phase, abort_v, err_flag);
         if (!__all_sync(0xffffffffu, ok)) break;
         const float2 *P = buf + (size_t)b * kApplyTileAmps;
         const ApplyStep stp = sstep[st];
         const IDX base = (IDX)((tile << kApplyTileBits) | (uint64_t)tid);   // bits 9-11 clear
         for (int g = stp.g_first; g < stp.g_first + stp.g_count; ++g) {
             const TileGroup &G = sgrp[g];
+            if (G.flat) {
+                float re = 0.0f, im = 0.0f;
+                for (int k = G.m[0]; k < G.m[8]; ++k) {
+                    const TileTerm<IDX> t = sterm[k];
+                    const uint32_t par = (uint32_t)(sizeof(IDX) == 4 ? __popc((uint32_t)(base & t.z))
+                                                                    : __popcll((uint64_t)(base & t.z)));
+                    const uint32_t sb = par << 31;
+                    re += __uint_as_float(__float_as_uint(t.re) ^ sb);
+                    im += __uint_as_float(__float_as_uint(t.im) ^ sb);
+                }
+                const float2 f = make_float2(re, im);
+#pragma unroll
+                for (int j = 0; j < kApplyTilePer; ++j)
+                    acc[j] = Cx<float>::fma(f, P[(uint32_t)(tid + j * kApplyTileThreads) ^ G.xl], acc[j]);
+                continue;
+            }
             float2 A[8];
 #pragma unroll
             for (int m = 0; m < 8; ++m) {
@@ -1034,10 +1057,16 @@ __global__ void __launch_bounds__(kApplyBlockThreads, 1)
         }
         __syncwarp();
         if (lane == 0) mbar_arrive(empty + b);   // this warp is done with buffer b
-        if (st == nsteps - 1) {
+        if (++b == kApplyTileBufs) {
+            b = 0;
+            phase ^= 1u;
+        }
+        if (++st == nsteps) {
 #pragma unroll
             for (int j = 0; j < kApplyTilePer; ++j)
                 o[(tile << kApplyTileBits) | (uint64_t)(tid + j * kApplyTileThreads)] = acc[j];
+            st = 0;
+            tile += gridDim.x;
         }
     }
 }
@@ -1132,6 +1161,7 @@ static Status launch_sumop_apply_tiles_f32(qi_state *o, qi_state *in, const std:
                 }
             }
             tg.m[8] = (int32_t)terms.size();
+            tg.flat = tg.m[1] == tg.m[8] ? 1 : 0;
             groups.push_back(tg);
         }
         steps.push_back(stp);

@@ -10,7 +10,7 @@
 //   [D_re | D_im][m] += Im X[.][m] . [-Im U ; Re U ]^T     (imaginary half)
 // The B operands are the R x R blocks -Im U, Re U, Im U stored one after the
 // other along N (K-major, shared memory), so [Re U ; Im U] starts at block 1
-// and [-Im U ; Re U] at block 0.  Pair mode (below), short of shared memory,
+// and [-Im U ; Re U] at block 0.  Pair mode with k = 6 (below), short of shared memory,
 // keeps only Re U, Im U and splits the imaginary half into two N = R products,
 //   D_re -= Im X . Im U^T (negate-B)   and   D_im += Im X . Re U^T.
 // Every operand is split as x = hi + lo with
@@ -205,8 +205,10 @@ struct TcCfg {
     static constexpr int UNIT_ROWS = 8;                // pair mode: rows per ring unit (one chunk)
     static constexpr int UNITS_PER_PAIR = 2 * CONV_ROWS / UNIT_ROWS;   // pair mode: 8
     static constexpr uint32_t BUF_BYTES = PAIR ? (uint32_t)UNIT_ROWS * 2 * 128 * sizeof(float2) : TILE_BYTES;
-    // operand blocks in shared memory: -Im U, Re U, Im U (hi, then lo); pair mode Re U, Im U
-    static constexpr int NBLK = PAIR ? 4 : 6;
+    // operand blocks in shared memory: -Im U, Re U, Im U (hi, then lo); pair mode with k = 6,
+    // short of shared memory, Re U, Im U (the imaginary half as two N = R products)
+    static constexpr bool SPLIT_IM = PAIR && K == 6;
+    static constexpr int NBLK = SPLIT_IM ? 4 : 6;
     static constexpr size_t OFF_TILES = (size_t)NBLK * BLK * sizeof(float);
     static constexpr size_t OFF_ROWX = OFF_TILES + (size_t)NBUF * BUF_BYTES;
     static constexpr size_t OFF_GROW = OFF_ROWX + 64 * sizeof(uint32_t);
@@ -305,7 +307,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_fused_tc(float2 *a, const flo
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
     // operand blocks -> shared memory (16-byte vectors), visible to the async proxy;
-    // pair mode takes blocks 1, 2, 4, 5 (Re U, Im U; hi then lo) of the six
+    // pair mode with k = 6 takes blocks 1, 2, 4, 5 (Re U, Im U; hi then lo) of the six
     {
         const uint4 *src = reinterpret_cast<const uint4 *>(blocks);
         uint4 *dst = reinterpret_cast<uint4 *>(sB);
@@ -634,7 +636,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_fused_tc(float2 *a, const flo
                         for (int j = 0; j < R / 8; ++j) {
                             const uint32_t kstep = (uint32_t)(2 * j) * C::LBO;
                             const uint32_t a_col = acol + (p == 2 ? R : 0) + 8 * j;
-                            if constexpr (!PAIR) {   // window [Re U ; Im U] (block 1) or [-Im U ; Re U] (block 0)
+                            if constexpr (!C::SPLIT_IM) {   // window [Re U ; Im U] (block 1) or [-Im U ; Re U] (block 0)
                                 const int blk = (p == 1 ? 3 : 0) + (h == 0 ? 1 : 0);
                                 const uint32_t boff = (uint32_t)(blk * C::BLK * 4) + kstep;
                                 mma_tf32_ts(dcol, a_col, desc0 + (uint64_t)(boff >> 4), idesc, (h | p | j) ? 1u : 0u);

@@ -251,7 +251,9 @@ qi_status qi_pauli_apply_exp(qi_state *s, const qi_pauli_term *t);
 qi_status qi_pauli_apply_exp_factor(qi_state *s, const qi_pauli_term *t, double factor_re, double factor_im);
 /* s = exp(-i dt coefficient P) |s>     PauliString::apply_exp_neg_i_dt pauli_string.rs:281-287 */
 qi_status qi_pauli_apply_exp_neg_i_dt(qi_state *s, const qi_pauli_term *t, double dt);
-/* out = sum_k c_k P_k |in>             SumOp::apply                   pauli_string.rs:453-466 */
+/* out = sum_k c_k P_k |in>             SumOp::apply                   pauli_string.rs:453-466
+ * Returns after the result is complete (it reads the output's device flag):
+ * QI_ERR_TIMEOUT if a bounded device-side wait of the streamed FP32 kernel ran out. */
 qi_status qi_sumop_apply(qi_state *out, qi_state *in, const qi_pauli_term *terms, int64_t n_terms);
 /* out = sum_k <s|c_k P_k|s>            SumOp::expectation_value       pauli_string.rs:485-507 */
 qi_status qi_sumop_expectation(qi_state *s, const qi_pauli_term *terms, int64_t n_terms, double out[2]);

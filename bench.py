@@ -822,6 +822,22 @@ def main():
                 link[name] = a.elapsed_time(b)
             link["h2d_gbs"] = 16 * dim / (link["h2d_ms"] / 1e3) / 1e9
             link["d2h_gbs"] = 16 * dim / (link["d2h_ms"] / 1e3) / 1e9
+            # the other public upload path: the GPU reads the page-locked buffer itself over the
+            # link, converting as it reads (qi_state_upload); it uses the SMs, so in the pipeline
+            # it adds to the circuit instead of overlapping it.  The pipeline takes the path whose
+            # predicted step is shorter on this machine's link.
+            torch.cuda.synchronize()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            st.upload_ptr(host_in.data_ptr(), dim)
+            b.record(stream)
+            torch.cuda.synchronize()
+            link["h2d_sm_ms"] = a.elapsed_time(b)
+            link["h2d_sm_gbs"] = 16 * dim / (link["h2d_sm_ms"] / 1e3) / 1e9
+            pred_ce = max(ms_per_step, link["h2d_ms"], link["d2h_ms"])
+            pred_sm = max(ms_per_step + link["h2d_sm_ms"], link["d2h_ms"])
+            sm_upload = pred_sm < 0.95 * pred_ce
+            link["predicted_step_ms"] = {"copy_engine_upload": pred_ce, "sm_upload": pred_sm}
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         e0 = torch.cuda.Event(enable_timing=True)
@@ -835,7 +851,10 @@ def main():
             circuit_end = []
             for k in range(e2e_steps):
                 s2, other = states[k % 2], states[(k + 1) % 2]
-                s2.upload_async(host_in.data_ptr(), dim)
+                if sm_upload:
+                    s2.upload_ptr(host_in.data_ptr(), dim)
+                else:
+                    s2.upload_async(host_in.data_ptr(), dim)
                 if k > 0:
                     s2.wait_for(other)   # other's stream so far ends with its circuit
                 plan.execute(s2)
@@ -860,9 +879,12 @@ def main():
         e2e_ms = e0.elapsed_time(e1)
         e2e = {"value": LAYERS * e2e_steps / (e2e_ms / 1e3), "unit": "layers/s", "h2d_bytes_per_step": 16 * dim,
                "d2h_bytes_per_step": 16 * dim, "wall_s": wall, "steps": e2e_steps,
-               "pipeline": ("two device states, circuits in turn (qi_state_wait); each state's H2D and D2H on the "
-                            "copy engines overlap the other state's circuit" if pipelined
-                            else "one state, transfers in order")}
+               "pipeline": (("two device states, circuits in turn (qi_state_wait); " +
+                             ("uploads read by the GPU over the link (qi_state_upload, faster than the copy "
+                              "engine on this machine), downloads on the copy engine overlapping the other "
+                              "state's circuit" if sm_upload else
+                              "each state's H2D and D2H on the copy engines overlap the other state's circuit"))
+                            if pipelined else "one state, transfers in order")}
         if pipelined:
             ends = [e0.elapsed_time(c) for c in circuit_end]
             e2e["link"] = link

@@ -106,6 +106,10 @@ qi_status qi_state_synchronize(qi_state *s);
 /* Copy host amplitudes (interleaved f64 pairs) into the device state,
  * converting to the state's precision on the device.  The host buffer stays
  * caller-owned.  num_amps must equal 2^num_qubits (else InvalidNumberOfQubits).
+ * A page-locked buffer is read in the state's stream order after the call
+ * returns (into an FP32 state by the GPU itself, over the link, converting as it
+ * reads), so it must stay unchanged until qi_state_synchronize; pageable buffers
+ * are staged before the call returns.
  * Replaces the host->device half of execute_on_gpu (operator.rs:48-58). */
 qi_status qi_state_upload(qi_state *s, const double *amps, uint64_t num_amps);
 /* Copy the device state back as interleaved f64 pairs (operator.rs:137-147). */

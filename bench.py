@@ -789,9 +789,10 @@ def main():
     extra["expectation"] = expectation
 
     # end-to-end through the public API with host buffers: H2D of the initial state,
-    # the circuit, D2H of the final state, every step.  Two device states alternate:
-    # each step's upload and download run on the copy engine (page-locked buffers,
-    # qi_state_upload_async / download_async) while the other state's circuit runs.
+    # the circuit, D2H of the final state, every step.  Two device states alternate: each
+    # step's download runs on the copy engine (page-locked buffers) while the other state's
+    # circuit runs; the upload takes one of the two public paths, chosen by a short trial of
+    # each on this machine's link (below).
     e2e = None
     if rank == 0:
         dim = 1 << n
@@ -809,10 +810,12 @@ def main():
                 s2.upload_async(host_in.data_ptr(), dim)   # the device, so none may happen in the timed loop)
                 plan.execute(s2)
                 s2.synchronize()
-            # the host link on its own (copy engine, page-locked buffers): what the pipeline hides
+            # the host link on its own: the copy engine both ways, and the GPU reading the page-locked
+            # buffer itself over the link (qi_state_upload; converts as it reads, uses the SMs)
             link = {}
             for name, fn in (("h2d_ms", lambda: st.upload_async(host_in.data_ptr(), dim)),
-                             ("d2h_ms", lambda: st.download_async(host_out[0].data_ptr(), dim))):
+                             ("d2h_ms", lambda: st.download_async(host_out[0].data_ptr(), dim)),
+                             ("h2d_sm_ms", lambda: st.upload_ptr(host_in.data_ptr(), dim))):
                 torch.cuda.synchronize()
                 a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
                 a.record(stream)
@@ -820,36 +823,19 @@ def main():
                 b.record(stream)
                 torch.cuda.synchronize()
                 link[name] = a.elapsed_time(b)
-            link["h2d_gbs"] = 16 * dim / (link["h2d_ms"] / 1e3) / 1e9
-            link["d2h_gbs"] = 16 * dim / (link["d2h_ms"] / 1e3) / 1e9
-            # the other public upload path: the GPU reads the page-locked buffer itself over the
-            # link, converting as it reads (qi_state_upload); it uses the SMs, so in the pipeline
-            # it adds to the circuit instead of overlapping it.  The pipeline takes the path whose
-            # predicted step is shorter on this machine's link.
+            for k in ("h2d", "d2h", "h2d_sm"):
+                link[k + "_gbs"] = 16 * dim / (link[k + "_ms"] / 1e3) / 1e9
+
+        def run_pipeline(sm_upload, steps):
+            """`steps` circuits one after the other (each state waits for the other's circuit, not
+            for its download), each state's download and next upload overlapping the other state's
+            circuit; returns (device ms from the first upload to the last download, circuit end ms)."""
             torch.cuda.synchronize()
-            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            a.record(stream)
-            st.upload_ptr(host_in.data_ptr(), dim)
-            b.record(stream)
-            torch.cuda.synchronize()
-            link["h2d_sm_ms"] = a.elapsed_time(b)
-            link["h2d_sm_gbs"] = 16 * dim / (link["h2d_sm_ms"] / 1e3) / 1e9
-            pred_ce = max(ms_per_step, link["h2d_ms"], link["d2h_ms"])
-            pred_sm = max(ms_per_step + link["h2d_sm_ms"], link["d2h_ms"])
-            sm_upload = pred_sm < 0.95 * pred_ce
-            link["predicted_step_ms"] = {"copy_engine_upload": pred_ce, "sm_upload": pred_sm}
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        if pipelined:
-            # circuits one after the other (each state waits for the other's circuit, not for its
-            # download), so each runs at the full device rate while the other state's download and
-            # next upload use the copy engines
-            e2e_steps = max(2, args.steps)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
             circuit_end = []
-            for k in range(e2e_steps):
+            for k in range(steps):
                 s2, other = states[k % 2], states[(k + 1) % 2]
                 if sm_upload:
                     s2.upload_ptr(host_in.data_ptr(), dim)
@@ -863,30 +849,51 @@ def main():
                 circuit_end.append(ce)
                 if k > 0:
                     other.download_async(host_out[(k - 1) % 2].data_ptr(), dim)
-            states[(e2e_steps - 1) % 2].download_async(host_out[(e2e_steps - 1) % 2].data_ptr(), dim)
+            states[(steps - 1) % 2].download_async(host_out[(steps - 1) % 2].data_ptr(), dim)
             joined = torch.cuda.Event()
             joined.record(stream2)
             stream.wait_event(joined)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            return e0.elapsed_time(e1), [e0.elapsed_time(c) for c in circuit_end]
+
+        sm_upload = False
+        if pipelined:
+            trial = {}
+            for mode in (False, True):
+                ms, _ = run_pipeline(mode, 3)
+                trial["sm_upload" if mode else "copy_engine_upload"] = ms / 3
+            sm_upload = trial["sm_upload"] < trial["copy_engine_upload"]
+            link["trial_ms_per_step"] = trial
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        if pipelined:
+            # ten circuits at least, so that the pipeline's fill (the first upload) and drain
+            # (the last download) weigh less than in a five-step run
+            e2e_steps = max(10, args.steps)
+            e2e_ms, ends = run_pipeline(sm_upload, e2e_steps)
         else:   # not enough page-locked host memory for two output buffers: one state, in order
             e2e_steps = max(1, min(args.steps, 3))
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
             for _ in range(e2e_steps):
                 st.upload_ptr(host_in.data_ptr(), dim)
                 plan.execute(st)
                 st.download_ptr(host_in.data_ptr(), dim)
-        e1.record(stream)
-        torch.cuda.synchronize()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            e2e_ms = e0.elapsed_time(e1)
         wall = time.perf_counter() - t0
-        e2e_ms = e0.elapsed_time(e1)
         e2e = {"value": LAYERS * e2e_steps / (e2e_ms / 1e3), "unit": "layers/s", "h2d_bytes_per_step": 16 * dim,
                "d2h_bytes_per_step": 16 * dim, "wall_s": wall, "steps": e2e_steps,
                "pipeline": (("two device states, circuits in turn (qi_state_wait); " +
-                             ("uploads read by the GPU over the link (qi_state_upload, faster than the copy "
-                              "engine on this machine), downloads on the copy engine overlapping the other "
-                              "state's circuit" if sm_upload else
-                              "each state's H2D and D2H on the copy engines overlap the other state's circuit"))
+                             ("uploads read by the GPU over the link (qi_state_upload), downloads on the copy "
+                              "engine overlapping the other state's circuit" if sm_upload else
+                              "each state's H2D and D2H on the copy engines overlap the other state's circuit") +
+                             "; upload path chosen by a 3-step trial of each")
                             if pipelined else "one state, transfers in order")}
         if pipelined:
-            ends = [e0.elapsed_time(c) for c in circuit_end]
             e2e["link"] = link
             e2e["circuit_end_ms"] = [round(x, 1) for x in ends]
             e2e["steady_ms_per_step"] = (ends[-1] - ends[0]) / max(1, len(ends) - 1)

@@ -667,7 +667,9 @@ def main():
     plan = qi.Plan(n, qi.F32, gates, fusion=qi.FUSION_GREEDY, max_block_qubits=FUSED_K)
     plan_s = time.perf_counter() - t0
     stats = plan.stats()
-    stream = torch.cuda.Stream()
+    # high priority: in the e2e pipeline the uploads the GPU reads over the link run on the engine's
+    # lowest-priority stream, so the circuits get freed SMs first
+    stream = torch.cuda.Stream(priority=-1)
     st = qi.DeviceState(n, qi.F32)
     st.set_stream(stream.cuda_stream)
 
@@ -802,7 +804,7 @@ def main():
         host_in[1::2] = 0.0
         if pipelined:
             host_out = [torch.empty(2 * dim, dtype=torch.float64, pin_memory=True) for _ in range(2)]
-            stream2 = torch.cuda.Stream()
+            stream2 = torch.cuda.Stream(priority=-1)
             st2 = qi.DeviceState(n, qi.F32)
             st2.set_stream(stream2.cuda_stream)
             states = [st, st2]

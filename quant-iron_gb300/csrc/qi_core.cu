@@ -65,10 +65,11 @@ __global__ void k_convert(typename Cx<TO>::V2 *o, const typename Cx<TI>::V2 *in,
 
 // The same conversion for a buffer on the other side of the CPU-GPU link (mapped,
 // page-locked host memory): four independent 16-byte accesses in flight per
-// thread to cover the link's latency.
+// thread to cover the link's latency.  At most 32 registers a thread, so a block
+// fits on an SM beside a tensor-core block (448 threads x 128 registers).
 template <typename TO, typename TI>
-__global__ void __launch_bounds__(256) k_convert_link(typename Cx<TO>::V2 *o, const typename Cx<TI>::V2 *in,
-                                                      uint64_t n) {
+__global__ void __launch_bounds__(256, 8) k_convert_link(typename Cx<TO>::V2 *o, const typename Cx<TI>::V2 *in,
+                                                         uint64_t n) {
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     for (uint64_t i0 = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i0 < n; i0 += 4 * stride) {
         typename Cx<TI>::V2 v[4];
@@ -554,6 +555,12 @@ qi_status qi_state_destroy(qi_state *s) {
         if (s->d_flag) cudaFree(s->d_flag);
         if (s->d_staging) cudaFree(s->d_staging);
         if (s->d_scratch) cudaFree(s->d_scratch);
+        if (s->link_stream) {
+            cudaStreamSynchronize(s->link_stream);
+            cudaStreamDestroy(s->link_stream);
+        }
+        for (cudaEvent_t ev : s->link_ev)
+            if (ev) cudaEventDestroy(ev);
         if (s->own_stream) cudaStreamDestroy(s->own_stream);
     }
     delete s;
@@ -636,10 +643,32 @@ qi_status qi_state_upload(qi_state *s, const double *amps, uint64_t num_amps) {
         return publish(ok_status());
     }
     if (const void *dp = mapped_host_ptr(amps)) {   // pinned: one pass reads the host buffer and converts
-        k_convert_link<float, double><<<grid_for(num_amps), 256, 0, s->stream>>>((float2 *)s->amps,
+        // On the handle's lowest-priority link stream, ordered after and before the handle's stream by
+        // events, in short blocks (1024 amplitudes each, four 16-byte reads in flight per thread): a
+        // circuit on a higher-priority stream of another handle gets each SM back as soon as the
+        // blocks on it finish, and the upload fills what the circuit leaves free.
+        cudaError_t e = cudaSuccess;
+        if (!s->link_stream) {
+            int least = 0, greatest = 0;
+            e = cudaDeviceGetStreamPriorityRange(&least, &greatest);
+            if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&s->link_stream, cudaStreamNonBlocking, least);
+            for (int i = 0; i < 2 && e == cudaSuccess; ++i)
+                e = cudaEventCreateWithFlags(&s->link_ev[i], cudaEventDisableTiming);
+            if (e != cudaSuccess) return publish(cuda_status(e, "upload link stream"));
+        }
+        e = cudaEventRecord(s->link_ev[0], s->stream);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(s->link_stream, s->link_ev[0], 0);
+        if (e != cudaSuccess) return publish(cuda_status(e, "upload"));
+        const uint64_t blocks = (num_amps + 1023) / 1024;
+        k_convert_link<float, double><<<(unsigned)blocks, 256, 0, s->link_stream>>>((float2 *)s->amps,
                                                                                  (const double2 *)dp, num_amps);
         count_launch();
-        return publish(check_launch("k_convert_link"));
+        Status st = check_launch("k_convert_link");
+        if (!st.ok()) return publish(st);
+        e = cudaEventRecord(s->link_ev[1], s->link_stream);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(s->stream, s->link_ev[1], 0);
+        if (e != cudaSuccess) return publish(cuda_status(e, "upload"));
+        return publish(ok_status());
     }
     const uint64_t chunk = num_amps < kChunkAmps ? num_amps : kChunkAmps;
     Status st = ensure_staging(s, 2 * chunk * 16);

@@ -65,6 +65,8 @@ struct qi_state {
     size_t staging_bytes = 0;
     int *d_flag = nullptr;            // device-side error flag (ZeroNorm inside async sequences)
     void *d_scratch = nullptr;        // second state buffer for out-of-place permutations (lazy)
+    cudaStream_t link_stream = nullptr;   // lowest-priority stream of uploads the GPU reads over the link (lazy)
+    cudaEvent_t link_ev[2] = {nullptr, nullptr};   // orders it after, and before, this handle's stream
 
     uint64_t dim() const { return 1ull << n; }
     size_t amp_bytes() const { return prec == QI_F64 ? 16 : 8; }

@@ -453,13 +453,15 @@ def per_gate_leg(qi, workloads, stream, n, peak):
     return out
 
 
-def costmodel_eval(qi, workloads, torch, np, n_train=28, count=4000, qubits=range(28, 35), exhaustive_upto=30):
+def costmodel_eval(qi, workloads, torch, np, n_train=28, count=4000, qubits=range(28, 35), exhaustive_upto=30,
+                   per_size=3):
     """The learned-fusion configuration: the cost model trained on `count` engine-timed blocks
-    at n_train qubits, then seeded random circuits of the benchmark family (one per qubit count
-    in `qubits`, depth 20-60) planned three ways — greedy fixed-k, the learned choice, and (up to
+    at n_train qubits, then seeded random circuits of the benchmark family (`per_size` per qubit
+    count in `qubits`, depth 20-60) planned three ways — greedy fixed-k, the learned choice, and (up to
     `exhaustive_upto` qubits) exhaustive timing of every preset partition — compared by measured
     wall time, and the learned plan's infidelity against the FP64 per-gate path up to
-    33 qubits (FP64 at 34 qubits would need 256 GiB)."""
+    33 qubits (FP64 at 34 qubits would need 256 GiB); the exhaustive timing and the FP64 check run
+    on the first circuit of each qubit count."""
     from quant_iron_gb300 import costmodel
     t0 = time.perf_counter()
     X, y = costmodel.collect(n_train, count, seed=11)
@@ -488,11 +490,11 @@ def costmodel_eval(qi, workloads, torch, np, n_train=28, count=4000, qubits=rang
             best = min(best, time.perf_counter() - t1)
         return best * 1e3
 
-    for n in qubits:
-        depth = 20 + (7 * n) % 41
-        gates = workloads.random_circuit(n, depth, seed=100 + n)
+    for n, rep in ((n, rep) for n in qubits for rep in range(per_size)):
+        depth = 20 + (7 * n + 13 * rep) % 41
+        gates = workloads.random_circuit(n, depth, seed=100 + n + 1000 * rep)
         st = qi.DeviceState(n, qi.F32)
-        rec = {"qubits": n, "layers": depth, "gates": int(gates.size)}
+        rec = {"qubits": n, "layers": depth, "gates": int(gates.size), "seed": 100 + n + 1000 * rep}
         pg = qi.Plan(n, qi.F32, gates, fusion=qi.FUSION_GREEDY, max_block_qubits=6)
         rec["greedy_ms"] = timed(pg, st)
         t1 = time.perf_counter()
@@ -502,7 +504,7 @@ def costmodel_eval(qi, workloads, torch, np, n_train=28, count=4000, qubits=rang
         rec["learned_predicted_ms"] = pl.stats()["predicted_us"] / 1e3
         rec["learned_kernels"] = pl.stats()["n_kernels"]
         rec["greedy_kernels"] = pg.stats()["n_kernels"]
-        if n <= exhaustive_upto:
+        if n <= exhaustive_upto and rep == 0:
             ex = {}
             for k in (2, 3, 4, 5, 6):
                 for tc in ((0, 2) if k >= 5 else (2,)):
@@ -512,7 +514,7 @@ def costmodel_eval(qi, workloads, torch, np, n_train=28, count=4000, qubits=rang
             rec["exhaustive_ms"] = ex
             rec["exhaustive_best"] = min(ex, key=ex.get)
             rec["exhaustive_best_ms"] = ex[rec["exhaustive_best"]]
-        if n <= 33:
+        if n <= 33 and rep == 0:
             s64 = qi.DeviceState(n, qi.F64)
             s64.set_plus()
             qi.Plan(n, qi.F64, gates, fusion=qi.FUSION_NONE).execute(s64)
@@ -524,7 +526,10 @@ def costmodel_eval(qi, workloads, torch, np, n_train=28, count=4000, qubits=rang
         out["circuits"].append(rec)
         print(json.dumps(rec), file=sys.stderr, flush=True)
     c = out["circuits"]
-    out["summary"] = {"learned_over_greedy_wall": [x["learned_ms"] / x["greedy_ms"] for x in c],
+    ratios = [x["learned_ms"] / x["greedy_ms"] for x in c]
+    out["summary"] = {"circuits": len(c), "learned_over_greedy_wall": ratios,
+                      "geomean_learned_over_greedy": float(np.exp(np.mean(np.log(ratios)))),
+                      "worst_learned_over_greedy": max(ratios),
                       "learned_over_exhaustive_best": [x["learned_ms"] / x["exhaustive_best_ms"] for x in c
                                                        if "exhaustive_best_ms" in x],
                       "max_infidelity": max(x.get("learned_infidelity", 0.0) for x in c)}

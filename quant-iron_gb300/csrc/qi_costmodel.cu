@@ -192,6 +192,37 @@ static void candidate_features(int n, bool f32, const std::vector<Elem> &elems, 
     if (used_tc) *n_norm = 1;
 }
 
+// Kernels a block list lowers to (the rules of build_plan, qi_plan.cu): one per single, permutation
+// and dense block; a run of diagonal blocks is one phase-polynomial pass (two or more blocks, or one
+// of three or more qubits; otherwise the block's own pass), none when it follows a tensor-core block
+// of an FP32 plan, whose epilogue applies it.
+static int64_t lowered_kernels(const std::vector<Block> &blocks, const std::vector<Elem> &elems, int n, bool f32,
+                               bool tc) {
+    int64_t kern = 0;
+    bool prev_tc = false;
+    int run = 0, run_k = 0;
+    auto end_run = [&]() {
+        if (run >= 2 || (run == 1 && run_k >= 3)) kern += (f32 && prev_tc) ? 0 : 1;
+        else if (run == 1) kern += 1;
+        run = run_k = 0;
+    };
+    for (const Block &b : blocks) {
+        bool diag = !b.single && !b.perm;
+        for (int idx : b.members) diag = diag && elems[(size_t)idx].diagonal;
+        const int k = __builtin_popcountll(b.mask);
+        if (diag && f32) {
+            ++run;
+            run_k = std::max(run_k, k);
+            continue;
+        }
+        end_run();
+        ++kern;
+        prev_tc = !b.single && !b.perm && !diag && tc && f32 && k >= 5 && n >= k + 7;
+    }
+    end_run();
+    return kern;
+}
+
 bool learned_choice(qi_plan *p, const std::vector<Elem> &elems, int kmax, int *k_out, int *tc_out, double *ms_out) {
     Mlp &m = global_mlp();
     std::lock_guard<std::mutex> lk(m.mu);
@@ -237,10 +268,11 @@ bool learned_choice(qi_plan *p, const std::vector<Elem> &elems, int kmax, int *k
     const bool tc_ok = p->opts.use_tensor_cores != 2;
     double lp_ms = 0.0;
     const std::vector<Block> lp = learned_partition_locked(m, n, f32, tc_ok, elems, kmax, &lp_ms);
-    // Every block is one pass over the state, so a partition with more blocks than the greedy one
-    // at the same k is not taken on the model's word alone (at 34 qubits, four times the states the
-    // model was trained on, such a partition predicted faster ran 4 % slower).
-    if (!lp.empty() && lp.size() <= window_partition(elems, n, kmax).size()) {
+    // Every kernel is one pass over the state, so a partition that lowers to more kernels than the
+    // greedy one at the same k is not taken on the model's word alone: over 21 seeded circuits of
+    // 28-34 qubits, each learned plan with more kernels than greedy's ran 2-5 % slower.
+    if (!lp.empty() &&
+        lowered_kernels(lp, elems, n, f32, tc_ok) <= lowered_kernels(window_partition(elems, n, kmax), elems, n, f32, tc_ok)) {
         bool any_tc = false;
         for (const Block &b : lp) {
             if (b.single) continue;

@@ -485,6 +485,36 @@ using namespace qi;
         if (!qi_dev_.ok()) return publish(qi_dev_);                   \
     }
 
+// Transfers the GPU itself makes over the CPU-GPU link (page-locked, mapped host buffers) run on
+// the handle's lowest-priority link stream, ordered after and before the handle's stream by events,
+// in short blocks (1024 amplitudes each, four 16-byte accesses in flight per thread): a circuit on a
+// higher-priority stream of another handle gets each SM back as soon as the blocks on it finish, and
+// the transfer fills what the circuit leaves free.
+static unsigned link_blocks(uint64_t num_amps) { return (unsigned)((num_amps + 1023) / 1024); }
+
+template <typename Launch>
+static Status on_link_stream(qi_state *s, Launch launch) {
+    cudaError_t e = cudaSuccess;
+    if (!s->link_stream) {
+        int least = 0, greatest = 0;
+        e = cudaDeviceGetStreamPriorityRange(&least, &greatest);
+        if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&s->link_stream, cudaStreamNonBlocking, least);
+        for (int i = 0; i < 2 && e == cudaSuccess; ++i) e = cudaEventCreateWithFlags(&s->link_ev[i], cudaEventDisableTiming);
+        if (e != cudaSuccess) return cuda_status(e, "link stream");
+    }
+    e = cudaEventRecord(s->link_ev[0], s->stream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(s->link_stream, s->link_ev[0], 0);
+    if (e != cudaSuccess) return cuda_status(e, "link stream order");
+    launch(s->link_stream);
+    count_launch();
+    Status st = check_launch("k_convert_link");
+    if (!st.ok()) return st;
+    e = cudaEventRecord(s->link_ev[1], s->link_stream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(s->stream, s->link_ev[1], 0);
+    if (e != cudaSuccess) return cuda_status(e, "link stream order");
+    return ok_status();
+}
+
 extern "C" {
 
 qi_status qi_last_error(qi_error_info *out) {
@@ -643,32 +673,11 @@ qi_status qi_state_upload(qi_state *s, const double *amps, uint64_t num_amps) {
         return publish(ok_status());
     }
     if (const void *dp = mapped_host_ptr(amps)) {   // pinned: one pass reads the host buffer and converts
-        // On the handle's lowest-priority link stream, ordered after and before the handle's stream by
-        // events, in short blocks (1024 amplitudes each, four 16-byte reads in flight per thread): a
-        // circuit on a higher-priority stream of another handle gets each SM back as soon as the
-        // blocks on it finish, and the upload fills what the circuit leaves free.
-        cudaError_t e = cudaSuccess;
-        if (!s->link_stream) {
-            int least = 0, greatest = 0;
-            e = cudaDeviceGetStreamPriorityRange(&least, &greatest);
-            if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&s->link_stream, cudaStreamNonBlocking, least);
-            for (int i = 0; i < 2 && e == cudaSuccess; ++i)
-                e = cudaEventCreateWithFlags(&s->link_ev[i], cudaEventDisableTiming);
-            if (e != cudaSuccess) return publish(cuda_status(e, "upload link stream"));
-        }
-        e = cudaEventRecord(s->link_ev[0], s->stream);
-        if (e == cudaSuccess) e = cudaStreamWaitEvent(s->link_stream, s->link_ev[0], 0);
-        if (e != cudaSuccess) return publish(cuda_status(e, "upload"));
-        const uint64_t blocks = (num_amps + 1023) / 1024;
-        k_convert_link<float, double><<<(unsigned)blocks, 256, 0, s->link_stream>>>((float2 *)s->amps,
-                                                                                 (const double2 *)dp, num_amps);
-        count_launch();
-        Status st = check_launch("k_convert_link");
-        if (!st.ok()) return publish(st);
-        e = cudaEventRecord(s->link_ev[1], s->link_stream);
-        if (e == cudaSuccess) e = cudaStreamWaitEvent(s->stream, s->link_ev[1], 0);
-        if (e != cudaSuccess) return publish(cuda_status(e, "upload"));
-        return publish(ok_status());
+        const Status st = on_link_stream(s, [&](cudaStream_t ls) {
+            k_convert_link<float, double><<<link_blocks(num_amps), 256, 0, ls>>>((float2 *)s->amps,
+                                                                               (const double2 *)dp, num_amps);
+        });
+        return publish(st);
     }
     const uint64_t chunk = num_amps < kChunkAmps ? num_amps : kChunkAmps;
     Status st = ensure_staging(s, 2 * chunk * 16);
@@ -737,10 +746,10 @@ qi_status qi_state_download(qi_state *s, double *amps, uint64_t num_amps) {
         return publish(ok_status());
     }
     if (void *dp = mapped_host_ptr(amps)) {   // pinned: one pass converts and writes the host buffer
-        k_convert_link<double, float><<<grid_for(num_amps), 256, 0, s->stream>>>((double2 *)dp,
-                                                                                 (const float2 *)s->amps, num_amps);
-        count_launch();
-        Status st = check_launch("k_convert_link");
+        Status st = on_link_stream(s, [&](cudaStream_t ls) {
+            k_convert_link<double, float><<<link_blocks(num_amps), 256, 0, ls>>>((double2 *)dp,
+                                                                               (const float2 *)s->amps, num_amps);
+        });
         if (!st.ok()) return publish(st);
         cudaError_t e = cudaStreamSynchronize(s->stream);
         if (e != cudaSuccess) return publish(cuda_status(e, "download"));

@@ -333,6 +333,49 @@ static Op bitperm_op(const std::vector<Elem> &elems, const Block &b) {
     return op;
 }
 
+// Widen a dense k-qubit block (k < 5; local bit j <-> op.targets[j], ascending) to 5 qubits: the
+// lowest qubits outside it join as identity factors.  op.targets / op.k and the matrix M are
+// rewritten in place (local bits again ascending by qubit).
+static void pad_block_to_5(int n, Op &op, std::vector<cd> &M) {
+    const int k = op.k;
+    uint64_t mask = 0;
+    for (int j = 0; j < k; ++j) mask |= 1ull << op.targets[j];
+    uint64_t sel = mask;
+    for (int q = 0, need = 5 - k; q < n && need > 0; ++q)
+        if (!((mask >> q) & 1ull)) {
+            sel |= 1ull << q;
+            --need;
+        }
+    int qs[5], nq = 0;
+    for (int q = 0; q < 64 && nq < 5; ++q)
+        if ((sel >> q) & 1ull) qs[nq++] = q;
+    int src[5];   // new local bit -> old local bit, or -1 for a padding qubit
+    for (int j = 0; j < 5; ++j) {
+        src[j] = -1;
+        for (int i = 0; i < k; ++i)
+            if (op.targets[i] == qs[j]) src[j] = i;
+    }
+    const int od = 1 << k;
+    std::vector<cd> W((size_t)32 * 32, cd(0, 0));
+    for (int r = 0; r < 32; ++r)
+        for (int c = 0; c < 32; ++c) {
+            int ro = 0, co = 0;
+            bool same = true;
+            for (int j = 0; j < 5; ++j) {
+                const int rb = (r >> j) & 1, cb = (c >> j) & 1;
+                if (src[j] < 0) same = same && rb == cb;
+                else {
+                    ro |= rb << src[j];
+                    co |= cb << src[j];
+                }
+            }
+            if (same) W[(size_t)r * 32 + c] = M[(size_t)ro * od + co];
+        }
+    M.swap(W);
+    op.k = 5;
+    for (int j = 0; j < 5; ++j) op.targets[j] = qs[j];
+}
+
 Status build_plan(qi_plan *p, std::vector<Elem> &elems) {
     const int n = p->n;
     int fusion = p->opts.fusion;
@@ -488,14 +531,21 @@ Status build_plan(qi_plan *p, std::vector<Elem> &elems) {
                 flush();
                 op.kind = OP_FUSED;
                 op.mode = use_tc;
-                for (size_t i = 0; i < (size_t)dim * dim; ++i) p->mats.push_back(mb[bi][i]);
-                if (op.mode && p->prec == QI_F32 && k >= 5 && n >= k + 7) {
+                if (op.mode && p->prec == QI_F32 && (k == 3 || k == 4) && n >= 12) {
+                    // a 3- or 4-qubit block runs faster on the tensor cores as a 5-qubit block with the
+                    // identity on the lowest free qubits (30 qubits: 3.5 ms on the CUDA cores, 2.6-2.9 ms
+                    // padded; low padding qubits give the tile long row runs)
+                    pad_block_to_5(n, op, mb[bi]);
+                }
+                const int kk = op.k, dd = 1 << kk;
+                for (size_t i = 0; i < (size_t)dd * dd; ++i) p->mats.push_back(mb[bi][i]);
+                if (op.mode && p->prec == QI_F32 && kk >= 5 && n >= kk + 7) {
                     op.tc_offset = (int64_t)p->tc.size();
-                    tc_blocks(k, reinterpret_cast<const double *>(mb[bi].data()), p->tc);
+                    tc_blocks(kk, reinterpret_cast<const double *>(mb[bi].data()), p->tc);
                 }
             }
             p->ops.push_back(op);
-            p->stats.n_blocks_by_k[k]++;
+            p->stats.n_blocks_by_k[op.k]++;
             if (op.tc_offset >= 0) {
                 ++tc_blocks_since;
                 ++tc_total;

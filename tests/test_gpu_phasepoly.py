@@ -22,15 +22,20 @@ def test_phase_poly_plan_vs_oracle(qi, orc, n, kmax):
     gates = diag_mix(n, seed=n, layers=2)
     init = orc.execute(workloads.plus_state(n), n, workloads.random_circuit(n, 2, seed=n, with_qft=False))
     want = orc.execute(init, n, gates)
-    plan = qi.Plan(n, qi.F32, gates, fusion=qi.FUSION_GREEDY, max_block_qubits=kmax)
-    assert any(op["kind"] == 9 for op in plan.ops())
-    with qi.DeviceState(n, qi.F32) as st:
-        st.upload(init)
-        plan.execute(st)
-        got = st.download()
-    assert np.max(np.abs(got - want)) < 2e-6
-    # normalised infidelity: FP32 rounding of the other kernels also moves the norm by ~1e-8
-    assert 1 - abs(np.vdot(want, got)) ** 2 / np.vdot(got, got).real < 1e-9
+    # CUDA-core blocks: the polynomials run as their own passes; default: a polynomial after a
+    # tensor-core block (3- and 4-qubit blocks are widened to 5 qubits from 12 qubits up) rides on
+    # its epilogue
+    for tc in (2, 0):
+        plan = qi.Plan(n, qi.F32, gates, fusion=qi.FUSION_GREEDY, max_block_qubits=kmax, use_tensor_cores=tc)
+        if tc == 2:
+            assert any(op["kind"] == 9 for op in plan.ops())
+        with qi.DeviceState(n, qi.F32) as st:
+            st.upload(init)
+            plan.execute(st)
+            got = st.download()
+        assert np.max(np.abs(got - want)) < 2e-6
+        # normalised infidelity: FP32 rounding of the other kernels also moves the norm by ~1e-8
+        assert 1 - abs(np.vdot(want, got)) ** 2 / np.vdot(got, got).real < 1e-9
 
 
 @pytest.mark.parametrize("tensor_cores", [2, 1], ids=["standalone", "in_tc_epilogue"])

@@ -166,3 +166,32 @@ def test_tf32_rate_probe(qi):
     with qi.DeviceState(14, qi.F32) as st:
         st.set_plus()
         assert abs(st.norm_sqr() - 1.0) < 1e-6
+
+
+def test_small_dense_blocks_padded_to_five_qubits(qi, orc):
+    """A 3- or 4-qubit dense block of an FP32 plan runs as a 5-qubit tensor-core block with the
+    identity on the lowest free qubits; the result matches the oracle."""
+    from quant_iron_gb300.workloads import GateList
+    n = 14
+    for qubits in ([5, 9, 12], [1, 2, 7, 13], [0, 1, 2]):
+        gl = GateList()
+        rng = np.random.default_rng(len(qubits))
+        for _ in range(3):
+            for q in qubits:
+                gl.add("RY", [q], [], [rng.uniform(0, 6.28)])
+                gl.add("RZ", [q], [], [rng.uniform(0, 6.28)])
+            for a, b in zip(qubits[:-1], qubits[1:]):
+                gl.add("CNOT", [b], [a])
+        gates = gl.array()
+        init = rand_state(n, 3)
+        want = orc.execute(init, n, gates)
+        plan = qi.Plan(n, qi.F32, gates, fusion=qi.FUSION_GREEDY, max_block_qubits=6, use_tensor_cores=1)
+        dense = [o for o in plan.ops() if o["kind"] == 4]
+        assert len(dense) == 1 and dense[0]["k"] == 5 and dense[0].get("tensor_cores"), plan.ops()
+        assert set(qubits) <= set(dense[0]["targets"])
+        with qi.DeviceState(n, qi.F32) as st:
+            st.upload(init)
+            plan.execute(st)
+            got = st.download()
+        assert np.max(np.abs(got - want)) < 2e-6
+        assert 1 - abs(np.vdot(want, got)) ** 2 / np.vdot(got, got).real < 1e-10

@@ -509,8 +509,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_fused_tc(float2 *a, const flo
             tc_fence_after();
             float2 *out = a + (tile_base(g, t) | cx);   // column base; rows add disjoint bits
             const uint32_t dcol = tmem + lane_base + C::COL_D + d * C::STAGE;
-#pragma unroll
-            for (int c = 0; c < R / 16; ++c) {
+            auto chunk = [&](int c) {   // rows 16c .. 16c + 15
                 uint32_t vr[16], vi[16];
                 tmem_ld<16>(dcol + 16 * c, vr);
                 tmem_ld<16>(dcol + R + 16 * c, vi);
@@ -521,13 +520,16 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_fused_tc(float2 *a, const flo
                     if (lane == 0) mbar_arrive(d_empty + d);
                 }
                 if constexpr (PHASE) {
+                    uint32_t fc = pbase;   // the chunk's row bits 4.. (bits of c)
+#pragma unroll
+                    for (int j = 4; j < K; ++j)
+                        if ((c >> (j - 4)) & 1) fc += z[j];
 #pragma unroll
                     for (int i = 0; i < 16; ++i) {
-                        const int r = 16 * c + i;   // compile-time after unrolling
-                        uint32_t f = pbase + FR[r];
+                        uint32_t f = fc + FR[16 * c + i];
 #pragma unroll
-                        for (int j = 0; j < K; ++j)
-                            if ((r >> j) & 1) f += z[j];
+                        for (int j = 0; j < 4; ++j)
+                            if ((i >> j) & 1) f += z[j];
                         // the angle as a signed fraction of a turn, in [-pi, pi): the SFU's sin / cos
                         // (absolute error about 2^-21, the order of the FP32 state's own rounding)
                         float sn, cs;
@@ -555,7 +557,13 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_fused_tc(float2 *a, const flo
                     for (int i = 0; i < 16; ++i)
                         __stcs(out + grow[16 * c + i], make_float2(__uint_as_float(vr[i]), __uint_as_float(vi[i])));
                 }
-            }
+            };
+            // Not unrolled: the kernel's four roles run different code, and with the epilogue unrolled
+            // over its chunks the warps waited on instruction fetch ("no instruction" stalls 3.2-4.7
+            // per issue). Rolled, 30-qubit launches took 3.09 against 3.44 ms (pairs), 2.67 against
+            // 2.80 ms (single tiles) and, carrying a phase polynomial, 2.83 against 3.81 ms.
+#pragma unroll 1
+            for (int c = 0; c < R / 16; ++c) chunk(c);
         }
     } else if (warp == kProducerWarp) {
         // ------------------------------------------------ producer (one thread)

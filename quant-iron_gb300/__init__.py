@@ -358,8 +358,10 @@ def trotter_evolve(state, terms, dt, num_steps, order=1, observable=None, observ
     return [complex(energies[2 * k], energies[2 * k + 1]) for k in range(num_steps // observe_every)]
 
 
+# op kind -> the kernels one op launches (8, the renormalisation: k_norm_partial first, unless a
+# qubit permutation just before it summed the norm as it wrote)
 KERNEL_OF_OP_KIND = {1: "k_mat1", 2: "k_swap", 3: "k_mat2", 4: "k_fused", 5: "k_pauli_exp", 6: "k_pauli_exp+normalise",
-                     7: "k_diagk", 8: "k_norm_partial+k_normalise_apply", 9: "k_phase_poly",
+                     7: "k_diagk", 8: "k_finalize+k_normalise_apply|to", 9: "k_phase_poly",
                      10: "k_pauli_group_diag|k_pauli_group_pair", 11: "k_bitperm"}
 
 

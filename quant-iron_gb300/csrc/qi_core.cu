@@ -415,6 +415,10 @@ Status state_normalise_device_to_async(qi_state *s, void *out, const void *in) {
     Status st = norm_async(s, &nb);
     s->amps = home;
     if (!st.ok()) return st;
+    return state_normalise_to_from_partials_async(s, out, in, nb);
+}
+
+Status state_normalise_to_from_partials_async(qi_state *s, void *out, const void *in, unsigned nb) {
     k_finalize<<<1, 256, 0, s->stream>>>(s->d_partials, (int)nb, 1, s->d_result);
     count_launch();
     unsigned g = grid_for(s->dim());

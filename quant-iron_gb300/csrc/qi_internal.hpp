@@ -164,7 +164,9 @@ void affine_compose(AffineMap &m, const GateMatrix &gm);   // m := gate o m
 Status affine_gather_async(qi_state *s, void *out, const void *in, const AffineMap &m);
 // Qubit permutation (tiled through shared memory, coalesced on both sides):
 // out[j] = in[flip ^ sum_k bit k of j << perm[k]], out != in.
-Status bitperm_async(qi_state *s, void *out, const void *in, const int8_t *perm, uint64_t flip);
+// norm_nb != nullptr: also the norm partials of the permuted state in s->d_partials (*norm_nb rows)
+Status bitperm_async(qi_state *s, void *out, const void *in, const int8_t *perm, uint64_t flip,
+                     unsigned *norm_nb = nullptr);
 // The same permutation in place, as one SWAP per transposition of perm's cycles and one X per
 // flipped bit (used when no second state buffer can be allocated).
 Status bitperm_in_place_async(qi_state *s, const int8_t *perm, uint64_t flip);
@@ -172,6 +174,8 @@ Status bitperm_in_place_async(qi_state *s, const int8_t *perm, uint64_t flip);
 Status state_scratch(qi_state *s, void **out);
 // Divide in by its FP64 norm into out (out != in; a norm of 0 or 1 copies unchanged, 0 flags ZeroNorm).
 Status state_normalise_device_to_async(qi_state *s, void *out, const void *in);
+// the same with the norm partials of `in` already in s->d_partials (nb rows)
+Status state_normalise_to_from_partials_async(qi_state *s, void *out, const void *in, unsigned nb);
 
 Status validate_gate(int n, const qi_gate &g);
 // State::measure (state.rs:525-730) on s (caller holds s's mutex): basis change, FP64 outcome

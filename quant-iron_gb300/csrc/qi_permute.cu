@@ -139,9 +139,12 @@ template <int L> struct PermRun;
 template <> struct PermRun<5> { static constexpr int kTile = 1 << 10; };
 template <> struct PermRun<6> { static constexpr int kTile = 1 << 12; };
 
+// With `partials`, the block also sums |amplitude|^2 of what it writes (FP32 per tile and thread for
+// FP32 states, folded into FP64) into partials[blockIdx.x * 4]: the norm of the permuted state for
+// a renormalisation that follows, without a read pass of its own.
 template <typename V2, int L>
 __global__ void __launch_bounds__(256) k_bitperm(V2 *__restrict__ out, const V2 *__restrict__ in,
-                                                 const __grid_constant__ BitPermParams p) {
+                                                 const __grid_constant__ BitPermParams p, double *partials) {
     constexpr int TMAX = PermRun<L>::kTile, H = 1 << L, U = 4;
     __shared__ V2 tile[TMAX + TMAX / H];
     __shared__ uint64_t rd_lo[H], rd_hi[H], wr_lo[H], wr_hi[H];
@@ -189,6 +192,7 @@ __global__ void __launch_bounds__(256) k_bitperm(V2 *__restrict__ out, const V2 
     __syncthreads();
     const int te = 1 << p.nt, lmask = (1 << nlo) - 1;
     const int step = blockDim.x;
+    double acc = 0.0;
     for (uint64_t t = blockIdx.x; t < p.ntiles; t += gridDim.x) {
         uint64_t bj = 0, bs = p.flip;
         for (int b = 0; b < nnib; ++b) {
@@ -213,15 +217,23 @@ __global__ void __launch_bounds__(256) k_bitperm(V2 *__restrict__ out, const V2 
                 if (e0 + u * step < te) tile[d[u] + (d[u] >> L)] = v[u];
         }
         __syncthreads();
+        decltype(V2::x) tsum = 0;
         for (int e = threadIdx.x; e < te; e += step) {
             const int el = e & lmask, eh = e >> nlo;
-            out[bj | wr_lo[el] | wr_hi[eh]] = tile[e + (e >> L)];
+            const V2 w = tile[e + (e >> L)];
+            out[bj | wr_lo[el] | wr_hi[eh]] = w;
+            tsum += w.x * w.x + w.y * w.y;
         }
+        acc += (double)tsum;
         __syncthreads();
+    }
+    if (partials) {   // uniform over the grid
+        const double v = block_sum(acc);
+        if (threadIdx.x == 0) partials[(size_t)blockIdx.x * 4] = v;
     }
 }
 
-Status bitperm_async(qi_state *s, void *out, const void *in, const int8_t *perm, uint64_t flip) {
+Status bitperm_async(qi_state *s, void *out, const void *in, const int8_t *perm, uint64_t flip, unsigned *norm_nb) {
     const int n = s->n;
     if (n > 8 * kAffineMaxBytes) return err(QI_ERR_UNSUPPORTED, n, 8 * kAffineMaxBytes, "qubit permutation width");
     BitPermParams p;
@@ -253,9 +265,13 @@ Status bitperm_async(qi_state *s, void *out, const void *in, const int8_t *perm,
         }
     p.flip = flip;
     p.ntiles = 1ull << p.no;
-    const uint64_t g = std::max<uint64_t>(1, std::min<uint64_t>(p.ntiles, 152 * 4));
-    if (s->prec == QI_F32) k_bitperm<float2, 6><<<(unsigned)g, 256, 0, s->stream>>>((float2 *)out, (const float2 *)in, p);
-    else k_bitperm<double2, 5><<<(unsigned)g, 256, 0, s->stream>>>((double2 *)out, (const double2 *)in, p);
+    const uint64_t g = std::max<uint64_t>(1, std::min<uint64_t>(p.ntiles, 152 * 4));   // <= kReduceBlocks
+    double *partials = norm_nb ? s->d_partials : nullptr;
+    if (s->prec == QI_F32)
+        k_bitperm<float2, 6><<<(unsigned)g, 256, 0, s->stream>>>((float2 *)out, (const float2 *)in, p, partials);
+    else
+        k_bitperm<double2, 5><<<(unsigned)g, 256, 0, s->stream>>>((double2 *)out, (const double2 *)in, p, partials);
+    if (norm_nb) *norm_nb = (unsigned)g;
     count_launch();
     return check_launch("k_bitperm");
 }

@@ -624,15 +624,23 @@ struct PlanRunner {
     qi_plan *p;
     qi_state *s;
     void *home;
+    unsigned norm_nb = 0;   // norm partials of the current amplitudes are in s->d_partials (rows)
     PlanRunner(qi_plan *p_, qi_state *s_) : p(p_), s(s_), home(s_->amps) {}
-    Status op(const Op &o) {
+    Status op(const Op &o, int next_kind) {
+        const unsigned have_norm = norm_nb;   // left by the op before this one
+        norm_nb = 0;
         if (o.kind == OP_BITPERM) {
             void *scratch = nullptr;
             if (s->amps == home && !state_scratch(s, &scratch).ok())
                 return bitperm_in_place_async(s, o.perm, o.xmask);   // no room for a second buffer
             void *dst = s->amps == home ? scratch : home;
-            Status st = bitperm_async(s, dst, s->amps, o.perm, o.xmask);
-            if (st.ok()) s->amps = dst;
+            // a renormalisation next: the permutation sums the norm as it writes
+            unsigned nb = 0;
+            Status st = bitperm_async(s, dst, s->amps, o.perm, o.xmask, next_kind == OP_NORMALISE ? &nb : nullptr);
+            if (st.ok()) {
+                s->amps = dst;
+                norm_nb = nb;
+            }
             return st;
         }
         if (o.kind == OP_MEASURE && s->amps != home) {   // measure the amplitudes in the state's own buffer
@@ -640,7 +648,8 @@ struct PlanRunner {
             if (!st.ok()) return st;
         }
         if (o.kind == OP_NORMALISE && s->amps != home) {
-            Status st = state_normalise_device_to_async(s, home, s->amps);
+            Status st = have_norm ? state_normalise_to_from_partials_async(s, home, s->amps, have_norm)
+                                  : state_normalise_device_to_async(s, home, s->amps);
             if (st.ok()) s->amps = home;
             return st;
         }
@@ -667,8 +676,9 @@ Status plan_execute(qi_plan *p, qi_state *s) {
     }
     bool has_norm = false;
     PlanRunner run(p, s);
-    for (const Op &op : p->ops) {
-        Status st = run.op(op);
+    for (size_t i = 0; i < p->ops.size(); ++i) {
+        const Op &op = p->ops[i];
+        Status st = run.op(op, i + 1 < p->ops.size() ? p->ops[i + 1].kind : -1);
         if (!st.ok()) return run.finish(st);
         has_norm = has_norm || op.kind == OP_PAULI_NORM;
     }
@@ -756,7 +766,7 @@ qi_status qi_plan_profile(qi_plan *p, qi_state *s, float *ms_out) {
     PlanRunner run(p, s);
     cudaEventRecord(ev[0], s->stream);
     for (size_t i = 0; i < nops && st.ok(); ++i) {
-        st = run.op(p->ops[i]);
+        st = run.op(p->ops[i], i + 1 < nops ? p->ops[i + 1].kind : -1);
         cudaEventRecord(ev[i + 1], s->stream);
     }
     st = run.finish(st);

@@ -398,3 +398,34 @@ def test_swap_x_runs_replay(qi, orc, seed):
     ops = plan.ops()
     assert sum(op["kind"] == 11 for op in ops) == expect
     assert np.max(np.abs(replay(ops, n, init) - want)) < 1e-12
+
+
+@pytest.mark.parametrize("qubits", [[5, 9, 12], [1, 2, 7, 13], [0, 1, 2]])
+def test_small_dense_blocks_widened_to_five_qubits(qi, orc, qubits):
+    """FP32 plans of 12 qubits and more widen a 3- or 4-qubit dense block to a 5-qubit tensor-core
+    block (identity on the lowest free qubits); the widened matrix replays to the oracle's result.
+    FP64 plans, plans without tensor cores and smaller states keep the block as it is."""
+    rng = np.random.default_rng(len(qubits))
+    gl = workloads.GateList()
+    for _ in range(3):
+        for q in qubits:
+            gl.add("RY", [q], [], [rng.uniform(0, 6.28)])
+            gl.add("RZ", [q], [], [rng.uniform(0, 6.28)])
+        for a, b in zip(qubits[:-1], qubits[1:]):
+            gl.add("CNOT", [b], [a])
+    gates = gl.array()
+    n = 14
+    init = workloads.plus_state(n)
+    want = orc.execute(init, n, gates)
+    ops = qi.Plan(n, qi.F32, gates, fusion=qi.FUSION_GREEDY, max_block_qubits=6).ops()
+    dense = [op for op in ops if op["kind"] == 4]
+    assert len(dense) == 1 and dense[0]["k"] == 5 and dense[0].get("tensor_cores")
+    free = [q for q in range(n) if q not in qubits][:5 - len(qubits)]
+    assert sorted(dense[0]["targets"]) == sorted(qubits + free)
+    assert np.max(np.abs(replay(ops, n, init) - want)) < 1e-12
+    for prec, nq, tc in ((qi.F64, 14, 0), (qi.F32, 14, 2), (qi.F32, 11, 0)):
+        g2 = gates if nq == 14 else np.array([g for g in gates if max(g["targets"][:1]) < nq], dtype=gates.dtype)
+        if nq != 14 and max(qubits) >= nq:
+            continue
+        ops2 = qi.Plan(nq, prec, g2, fusion=qi.FUSION_GREEDY, max_block_qubits=6, use_tensor_cores=tc).ops()
+        assert [op["k"] for op in ops2 if op["kind"] == 4] == [len(qubits)]

@@ -195,7 +195,8 @@ static void candidate_features(int n, bool f32, const std::vector<Elem> &elems, 
 // Kernels a block list lowers to (the rules of build_plan, qi_plan.cu): one per single, permutation
 // and dense block; a run of diagonal blocks is one phase-polynomial pass (two or more blocks, or one
 // of three or more qubits; otherwise the block's own pass), none when it follows a tensor-core block
-// of an FP32 plan, whose epilogue applies it.
+// of an FP32 plan, whose epilogue applies it (dense blocks of 3 or 4 qubits are widened to 5-qubit
+// tensor-core blocks from 12 qubits up).
 static int64_t lowered_kernels(const std::vector<Block> &blocks, const std::vector<Elem> &elems, int n, bool f32,
                                bool tc) {
     int64_t kern = 0;
@@ -217,7 +218,8 @@ static int64_t lowered_kernels(const std::vector<Block> &blocks, const std::vect
         }
         end_run();
         ++kern;
-        prev_tc = !b.single && !b.perm && !diag && tc && f32 && k >= 5 && n >= k + 7;
+        const int kt = (k == 3 || k == 4) && n >= 12 ? 5 : k;   // the width it runs at
+        prev_tc = !b.single && !b.perm && !diag && tc && f32 && kt >= 5 && n >= kt + 7;
     }
     end_run();
     return kern;

@@ -91,3 +91,35 @@ def test_in_place_fallback_matches(qi):
             torch.cuda.empty_cache()
         got = b.download()   # host transfers stage through device memory: after the release
     assert np.array_equal(got, want)
+
+
+@pytest.mark.parametrize("n", [16, 21])
+def test_renormalisation_after_a_permutation_uses_its_norm(qi, orc, n):
+    """Tensor-core blocks, then a SWAP network lowered to one permutation, then the plan's closing
+    renormalisation: the permutation sums the norm as it writes and the renormalisation scales with
+    it (no read pass of its own). The result matches the oracle and has unit norm."""
+    rng = np.random.default_rng(n)
+    gl = workloads.GateList()
+    for _ in range(4):
+        for q in range(n):
+            gl.add("RY", [q], [], [float(rng.uniform(0, 6.28))])
+            gl.add("RZ", [q], [], [float(rng.uniform(0, 6.28))])
+        for q in range(n - 1):
+            gl.add("CNOT", [q + 1], [q])
+    for q in range(n // 2):
+        gl.add("SWAP", [q, n - 1 - q])
+    gates = gl.array()
+    init = workloads.plus_state(n)
+    want = orc.execute(init, n, gates)
+    plan = qi.Plan(n, qi.F32, gates, fusion=qi.FUSION_GREEDY, max_block_qubits=6)
+    kinds = [op["kind"] for op in plan.ops()]
+    assert kinds[-2:] == [11, 8] and any(op["kind"] == 4 and op.get("tensor_cores") for op in plan.ops())
+    with qi.DeviceState(n, qi.F32) as st:
+        st.upload(init)
+        p0 = st.device_ptr()
+        plan.execute(st)
+        got = st.download()
+        assert st.device_ptr() == p0
+        assert abs(st.norm_sqr() - 1.0) < 1e-6
+    assert np.max(np.abs(got - want)) < 2e-6
+    assert 1 - abs(np.vdot(want, got)) ** 2 / np.vdot(got, got).real < 1e-10
